@@ -1,0 +1,338 @@
+"""Benchmark of the explicit impact step: element-steps/s on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload shell|quad|small]
+                    [--impl ours|reference]
+
+Default workload: the large thin shell -- a cylinder R = 1 m, L = 4 m, t = 4 mm,
+720 x 140 x 1 cells x 6 Kuhn tets = 604,800 tet10 elements, 1,213,920 nodes, aluminium
+J2 (E 68.9 GPa, nu 0.33, rho 2700, sigma_y0 276 MPa, H 0.689 GPa), 5 m/s onto the
+tangent plane, dt = 0.5 CFL, seeded synthetic mesh.  One "step" is one full solver
+step (element internal force + J2 update, force assembly, contact, central-difference
+update) over the whole mesh; the working set (~0.3 GB per step) exceeds L2, so no
+flush is needed between steps.
+
+Our arm prints one JSON line with value (device-resident, CUDA events on the solver's
+stream), e2e (through the C ABI with host buffers and the copies inside the timed
+region), the roofline of the dominant kernel, the CPU baseline and sampled clocks.
+The reference arm (--impl reference) times the reference's CPU algorithm -- the
+oracle's restatement of it, since the reference's compiled code cannot travel -- with
+all host threads on a bounded sample of the same workload.
+
+Under torchrun (N > 1) every rank runs its own replica (the step does not shard
+across GPUs without a halo exchange; replicas only) and rank 0 reports the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("element-steps/s on 1 GB300 vs plain GPU & host CPU; sweep runs/hr at "
+          "≤2% peak-disp err")
+UNIT = "element-steps/s"
+MAT = dict(E=68.9e9, nu=0.33, rho=2700.0, sigma_y0=276e6, H=0.689e9)
+
+
+def workload(name: str):
+    from cppimpact_gb300 import meshgen as mg
+    if name == "shell":
+        m = mg.shell()
+        setup = mg.impact_setup(m, 5.0, 0.0)
+        desc = "shell R1 L4 t0.004 720x140x1 tet10 J2 5 m/s"
+    elif name == "quad":
+        m = mg.cube(18, 2)
+        setup = mg.impact_setup(m, 20.0, 1e-3)
+        desc = "cube 18^3x6 tet10 J2 20 m/s"
+    else:
+        m = mg.cube(10, 1)
+        setup = mg.impact_setup(m, 10.0, 1e-3)
+        desc = "cube 10^3x6 tet4 J2 10 m/s"
+    return m, setup, desc
+
+
+def algorithmic_bytes(npe: int, E: int, N: int):
+    """Per step: 4 npe + 56 nq per element + 112 per node (X0 fp32, u/v fp64 r/w, m fp32).
+    The element kernel alone: connectivity + stress state r/w + X0, u, v reads."""
+    nq = 1 if npe == 4 else 4
+    step = E * (4 * npe + 56 * nq) + 112 * N
+    elem_kernel = E * (4 * npe + 56 * nq) + 60 * N
+    return step, elem_kernel
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus: int):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(m, setup, seconds_budget: float = 15.0, threads: int | None = None):
+    """The reference's CPU algorithm (restated in oracle/ref_port.cpp: 5-point K_e,
+    dense gemv, row-sum mass, z-wall) on a bounded sample: whole solver steps over the
+    first elements of the mesh, all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py as op
+    threads = threads or os.cpu_count() or 1
+    E = m.num_elements
+    # probe: one step on a small slice sizes the sample to the budget
+    def run(ne, nsteps):
+        conn = m.conn[:ne]
+        used = np.unique(conn)
+        remap = np.full(m.num_nodes, -1, np.int32)
+        remap[used] = np.arange(used.size, dtype=np.int32)
+        x = m.xloc[used]
+        c = remap[conn]
+        rp = op.ref_params(MAT["E"], MAT["nu"], MAT["rho"], setup["wall_offset"],
+                           setup["wall_stiffness"], 1)
+        t0 = time.perf_counter()
+        op.ref_solve(x, c, rp, setup["vel"], setup["dt"], (nsteps - 1) * setup["dt"] + 0.5 * setup["dt"],
+                     nthreads=threads)
+        return time.perf_counter() - t0
+    ne = min(E, 4096)
+    t = run(ne, 1)
+    per_elem_step = t / (ne * 2)  # initial update + one step
+    ne = int(min(E, max(ne, seconds_budget / 2 / per_elem_step)))
+    nsteps = 1
+    t = run(ne, nsteps)
+    value = ne * (nsteps + 1) / t
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{ne} of {E} elements (first in mesh order), {nsteps + 1} updates "
+                      f"(initial + {nsteps} step), RefCompat 5-point K_e, {t:.1f} s"}
+
+
+def run_ours(args, rank, world):
+    from cppimpact_gb300 import api
+    m, setup, desc = workload(args.workload)
+    N, E, npe = m.num_nodes, m.num_elements, m.npe
+    s = api.Solver(m.xloc, m.conn, **MAT, mode=api.MODE_J2, lumping=api.LUMP_HRZ,
+                   wall_normal=setup["wall_normal"], wall_offset=setup["wall_offset"],
+                   wall_stiffness=setup["wall_stiffness"],
+                   device=int(os.environ.get("LOCAL_RANK", "0")))
+    s.initialize(setup["vel"])
+    s.start(setup["dt"])
+    s.step(max(args.warmup, 3))
+    # device-resident timed region: K steps, CUDA events on the solver's stream
+    barrier(world)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ms = s.time_steps(args.steps)
+    barrier(world)
+    ms = max_over_ranks(ms, world)
+    ms_step = ms / args.steps
+    value = world * E * args.steps / (ms / 1e3)
+    # per-kernel device durations (separate pass, per-launch events)
+    k_elem_ms, k_node_ms = s.time_kernels(min(args.steps, 200))
+    step_bytes, elem_bytes = algorithmic_bytes(npe, E, N)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    achieved = elem_bytes / (k_elem_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_elem (element force + J2 + colour assembly)",
+                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_src,
+                "traffic": args.traffic, "kernel_ms": round(k_elem_ms, 4),
+                "node_kernel_ms": round(k_node_ms, 4),
+                "bytes_formula": "E(4 npe + 56 nq) + 60 N"}
+    step_roof = {"achieved": round(step_bytes / (ms_step * 1e-3) / 1e9, 1),
+                 "frac": round(step_bytes / (ms_step * 1e-3) / 1e9 / peak, 4),
+                 "bytes_per_elem_step": round(step_bytes / E, 1)}
+    # end to end through the C ABI with host buffers: per call, upload the state,
+    # advance S steps, read the state back (an export interval of the reference driver)
+    S = args.e2e_interval
+    x0 = np.ascontiguousarray(m.xloc, dtype=np.float64)
+    st = s.state(fields=("x", "v"))
+    xh, vh = st["x"], st["v"]
+    calls = max(1, args.steps // S)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        s.set_state(xh, vh)
+        s.step(S)
+        out = s.state(fields=("x", "v"))
+        xh, vh = out["x"], out["v"]
+    t1 = time.perf_counter()
+    barrier(world)
+    e2e_s = max_over_ranks(t1 - t0, world)
+    e2e = {"value": world * E * S * calls / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": 48 * N / S, "d2h_bytes_per_step": 48 * N / S,
+           "steps_per_call": S,
+           "api": "per call: ci_set_state(x, v) + ci_step(S) + ci_get_state(x, v), host buffers"}
+    en = s.energy()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "state_dtype": "f64",
+        "data": "synthetic (seeded mesh, seed 20261203)",
+        "config": {"workload": desc, "elements": E, "nodes": N, "nodes_per_element": npe,
+                   "dt": setup["dt"], "l2": "working set > L2 (no flush)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": roofline, "step_roofline": step_roof, "e2e": e2e,
+        "gpu_launches": s.launches_per_step() * args.steps,
+        "clocks": clk.summary(),
+        "energy_balance_rel": abs(en["balance"]) / max(en["kinetic0"], 1e-300),
+    }
+    s.close()
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(m, setup, args.cpu_seconds)
+    return line
+
+
+def run_reference(args, rank, world):
+    m, setup, desc = workload(args.workload)
+    if rank != 0:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py as op
+    threads = os.cpu_count() or 1
+    E = m.num_elements
+    # bounded sample sized so that each step takes ~0.5 s on this host
+    probe = cpu_baseline(m, setup, seconds_budget=2.0, threads=threads)
+    ne = int(min(E, max(1024, probe["value"] * 0.5)))
+    conn = m.conn[:ne]
+    used = np.unique(conn)
+    remap = np.full(m.num_nodes, -1, np.int32)
+    remap[used] = np.arange(used.size, dtype=np.int32)
+    x, c = m.xloc[used], remap[conn]
+    rp = op.ref_params(MAT["E"], MAT["nu"], MAT["rho"], setup["wall_offset"],
+                       setup["wall_stiffness"], 1)
+    dof = np.zeros(3 * used.size)
+    rng = np.random.default_rng(1)
+    dof += rng.normal(scale=1e-7, size=dof.size)
+    for _ in range(max(args.warmup, 0)):
+        op.ref_update(x, c, rp, dof, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        op.ref_update(x, c, rp, dof, nthreads=threads)
+    t = time.perf_counter() - t0
+    value = ne * args.steps / t
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded mesh, seed 20261203)",
+        "config": {"workload": desc, "elements": E, "nodes": m.num_nodes,
+                   "nodes_per_element": m.npe, "dt": setup["dt"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{ne} of {E} elements per step (one reference update: "
+                                   f"5-point K_e, gemv, scatter, wall), {args.steps} steps"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--workload", default="shell", choices=["shell", "quad", "small"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-interval", type=int, default=100)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="dram bytes per element-kernel launch from an ncu capture")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world = dist_setup(args.gpus)
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world)
+    if rank == 0 and line is not None:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

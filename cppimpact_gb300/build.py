@@ -1,0 +1,76 @@
+"""Builds libcppimpact_gb300.so in-tree for sm_103a (no cmake, a few seconds per file).
+
+    python -m cppimpact_gb300.build        # or build() from Python
+
+Host translation units are compiled with g++, the CUDA one with nvcc
+``-gencode arch=compute_103a,code=sm_103a -lineinfo``, all in parallel, then linked
+with nvcc into ``cppimpact_gb300/libcppimpact_gb300.so``.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libcppimpact_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+HOST_SOURCES = ["ci_plan.cpp", "ci_inp.cpp"]
+CUDA_SOURCES = ["ci_solver.cu"]
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return cand
+
+
+def _stale(obj: str, deps: list[str]) -> bool:
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers.append(os.path.join(ROOT, "include", "cppimpact_gb300.h"))
+    jobs, objs = [], []
+    for src in HOST_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if _stale(o, [s] + headers):
+            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-c", s, "-o", o])
+    for src in CUDA_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if _stale(o, [s] + headers):
+            jobs.append([_nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "--expt-relaxed-constexpr", *(extra_nvcc or []), "-c", s, "-o", o])
+    procs = [(j, subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
+             for j in jobs]
+    failed = False
+    for j, p in procs:
+        out, _ = p.communicate()
+        if verbose or p.returncode != 0:
+            sys.stderr.write(" ".join(j) + "\n" + (out or ""))
+        failed |= p.returncode != 0
+    if failed:
+        raise RuntimeError("libcppimpact_gb300 build failed")
+    if jobs or not os.path.exists(LIB):
+        link = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        r = subprocess.run(link, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,504 @@
+// ci_kernels.cuh -- sm_103a kernels of the explicit impact step.
+//
+// K1 k_elem   : one CTA per chunk (see ci_plan.h).  Stages the chunk's nodes in shared
+//               memory (reference coordinates relative to the chunk origin + FP64
+//               displacement rounded to FP32; increment dt v), computes the element
+//               internal force matrix-free in FP32 (FEAnalysis::calculate_f_internal,
+//               include/analysis.h:321-382, without forming B or K_e), updates the J2
+//               state, accumulates node forces in shared memory colour by colour and
+//               writes one partial sum per (chunk, local node) slot.
+// K2 k_node   : one thread per node.  Sums the node's slots in chunk order, a = -f/m,
+//               planar penalty wall and gravity (include/dynamics_kernels.h:150-168,
+//               include/wall.h:37-43), FP64 central-difference update
+//               (include/dynamics.h:477-503).
+// K3 k_elem<MASS_*> + k_mass_sum : lumped mass, once (include/analysis.h:136-162).
+//
+// No float atomics anywhere: every floating-point sum has a fixed order.
+#pragma once
+#include <cstdint>
+
+#include "ci_plan.h"
+
+namespace ci {
+
+enum ElemMode { EM_J2 = 0, EM_REFCOMPAT = 1, EM_MASS_ROWSUM = 2, EM_MASS_HRZ = 3 };
+
+enum StatusBits { ST_DEGENERATE = 1u, ST_NONFINITE = 2u };
+
+struct DevPlan {
+  const ChunkInfo* chunks;
+  const uint16_t* conn_local;  // [npe][E]
+  const uint8_t* color;        // [E]
+  const int* local_gid;        // [Lt]
+  const int* local_slot;       // [Lt]
+  const float* local_x0;       // [3][Lt] reference coordinates relative to the chunk origin
+  const int* slot_row;         // [N+1]
+  int E, N, Lt;
+};
+
+struct DevState {
+  double* u[3];        // displacement from the reference positions, SoA [N]
+  double* v[3];        // half-step velocity, SoA [N]
+  float* slot_f[3];    // partial node forces per slot, SoA [S]
+  float4* sig_a;       // [nq][E] stress xx yy zz xy
+  float2* sig_b;       // [nq][E] stress yz xz
+  float* epbar;        // [nq][E] equivalent plastic strain
+  double* chunk_work;  // [C][4] internal work, plastic work, volume, unused (running sums)
+  unsigned int* status;
+};
+
+struct ElemParams {
+  float dt;
+  float lambda, mu;       // Lame constants
+  float sy0, H;           // yield stress, hardening modulus
+  float rho;
+  int accum_energy;       // accumulate work terms into chunk_work
+};
+
+struct NodeParams {
+  double dt;
+  double g[3];
+  double wall_n[3];
+  double wall_k;
+  int N;
+};
+
+struct NodeArrays {
+  double* u[3];
+  double* v[3];
+  const float* slot_f[3];
+  const int* slot_row;
+  const float* mass;
+  const double* d0;        // wall_n . X - wall_offset per node
+  unsigned char* contact;  // bit0 current, bit1 ever
+  float* acc[3];           // last acceleration (written when STORE_ACC)
+  unsigned int* status;
+};
+
+// ---------------------------------------------------------------------------
+// Element geometry: the reference parametrisation (include/tetrahedral.h:182-250,
+// 521-549): barycentrics L = (xi, eta, 1-xi-eta-zeta, zeta) for corners 0..3 and the
+// CalculiX edge order 4:(0,1) 5:(1,2) 6:(2,0) 7:(0,3) 8:(1,3) 9:(2,3).
+// ---------------------------------------------------------------------------
+template <int NPE>
+struct Rule;
+
+template <>
+struct Rule<4> {
+  static constexpr int NQ = 1;
+  static constexpr float W = 1.0f / 6.0f;
+  __device__ __forceinline__ static void grad(int, float G[4][3]) {
+    G[0][0] = -1.f; G[0][1] = -1.f; G[0][2] = -1.f;
+    G[1][0] = 1.f;  G[1][1] = 0.f;  G[1][2] = 0.f;
+    G[2][0] = 0.f;  G[2][1] = 1.f;  G[2][2] = 0.f;
+    G[3][0] = 0.f;  G[3][1] = 0.f;  G[3][2] = 1.f;
+  }
+  __device__ __forceinline__ static void shape(int, float N[4]) {
+    N[0] = N[1] = N[2] = N[3] = 0.25f;
+  }
+};
+
+template <>
+struct Rule<10> {
+  // 4-point Gauss rule, degree 2: a = (5 + 3 sqrt5)/20, b = (5 - sqrt5)/20, w = 1/24.
+  static constexpr int NQ = 4;
+  static constexpr float W = 1.0f / 24.0f;
+  __device__ __forceinline__ static void bary(int q, float L[4]) {
+    const float a = 0.58541019662496845f, b = 0.13819660112501052f;
+    // QP q has parametric point (b,b,b), (a,b,b), (b,a,b), (b,b,a)
+    const float xi = q == 1 ? a : b, eta = q == 2 ? a : b, zeta = q == 3 ? a : b;
+    L[0] = xi;
+    L[1] = eta;
+    L[2] = q == 0 ? a : b;  // 1 - xi - eta - zeta
+    L[3] = zeta;
+  }
+  __device__ __forceinline__ static void grad(int q, float G[10][3]) {
+    float L[4];
+    bary(q, L);
+    const float dL[4][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {-1.f, -1.f, -1.f}, {0.f, 0.f, 1.f}};
+    const int ea[6] = {0, 1, 2, 0, 1, 2}, eb[6] = {1, 2, 0, 3, 3, 3};
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) G[c][j] = (4.f * L[c] - 1.f) * dL[c][j];
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        G[4 + k][j] = 4.f * (L[ea[k]] * dL[eb[k]][j] + L[eb[k]] * dL[ea[k]][j]);
+  }
+  __device__ __forceinline__ static void shape(int q, float N[10]) {
+    float L[4];
+    bary(q, L);
+    const int ea[6] = {0, 1, 2, 0, 1, 2}, eb[6] = {1, 2, 0, 3, 3, 3};
+#pragma unroll
+    for (int c = 0; c < 4; c++) N[c] = L[c] * (2.f * L[c] - 1.f);
+#pragma unroll
+    for (int k = 0; k < 6; k++) N[4 + k] = 4.f * L[ea[k]] * L[eb[k]];
+  }
+};
+
+// Cofactor inverse of a 3x3 (row-major), returns det (cf. inv3x3, include/physics.h:38-58).
+__device__ __forceinline__ float inv3f(const float* A, float* Ai) {
+  const float c00 = A[4] * A[8] - A[5] * A[7];
+  const float c01 = A[5] * A[6] - A[3] * A[8];
+  const float c02 = A[3] * A[7] - A[4] * A[6];
+  const float det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+  const float r = __frcp_rn(det);
+  Ai[0] = c00 * r;
+  Ai[1] = (A[2] * A[7] - A[1] * A[8]) * r;
+  Ai[2] = (A[1] * A[5] - A[2] * A[4]) * r;
+  Ai[3] = c01 * r;
+  Ai[4] = (A[0] * A[8] - A[2] * A[6]) * r;
+  Ai[5] = (A[2] * A[3] - A[0] * A[5]) * r;
+  Ai[6] = c02 * r;
+  Ai[7] = (A[1] * A[6] - A[0] * A[7]) * r;
+  Ai[8] = (A[0] * A[4] - A[1] * A[3]) * r;
+  return det;
+}
+
+// J2 radial return with linear isotropic hardening (Simo & Hughes 1998, Box 3.1):
+// trial = s + lambda tr(de) I + 2 mu de (engineering shear in de[3..5]); if the
+// deviatoric norm exceeds sqrt(2/3)(sy0 + H epbar), return along the deviator.
+__device__ __forceinline__ void j2_return(const ElemParams& p, float s[6], float& epbar) {
+  const float pm = (s[0] + s[1] + s[2]) * (1.0f / 3.0f);
+  const float d0 = s[0] - pm, d1 = s[1] - pm, d2 = s[2] - pm;
+  const float nrm2 = d0 * d0 + d1 * d1 + d2 * d2 + 2.f * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]);
+  const float nrm = sqrtf(nrm2);
+  const float f = nrm - 0.81649658092772603f * (p.sy0 + p.H * epbar);
+  if (f > 0.f) {
+    const float dg = f / (2.f * p.mu + (2.f / 3.f) * p.H);
+    const float sc = 1.f - 2.f * p.mu * dg / nrm;
+    s[0] = d0 * sc + pm;
+    s[1] = d1 * sc + pm;
+    s[2] = d2 * sc + pm;
+    s[3] *= sc;
+    s[4] *= sc;
+    s[5] *= sc;
+    epbar += 0.81649658092772603f * dg;
+  }
+}
+
+// Element internal force (and J2 update) for element e at plan position e.
+// x: current coordinates relative to the chunk origin, du: increment.
+template <int NPE, int MODE>
+__device__ __forceinline__ void element_force(const ElemParams& p, const DevState& S, int e, int E,
+                                              const float (&x)[NPE][3], const float (&du)[NPE][3],
+                                              float (&f)[NPE][3], float& wint, float& wp,
+                                              float& vol) {
+  using R = Rule<NPE>;
+#pragma unroll
+  for (int i = 0; i < NPE; i++) f[i][0] = f[i][1] = f[i][2] = 0.f;
+#pragma unroll
+  for (int q = 0; q < R::NQ; q++) {
+    float G[NPE][3];
+    R::grad(q, G);
+    float J[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) J[k] = 0.f;
+#pragma unroll
+    for (int i = 0; i < NPE; i++)
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) J[3 * a + j] = fmaf(x[i][a], G[i][j], J[3 * a + j]);
+    float Ji[9];
+    const float detJ = inv3f(J, Ji);
+    if (!(detJ > 0.f)) atomicOr(S.status, (unsigned)ST_DEGENERATE);
+    const float wd = R::W * detJ;
+    vol += wd;
+    if (MODE == EM_MASS_ROWSUM || MODE == EM_MASS_HRZ) {
+      float N[NPE];
+      R::shape(q, N);
+#pragma unroll
+      for (int i = 0; i < NPE; i++) f[i][0] = fmaf(p.rho * wd, N[i], f[i][0]);
+      continue;
+    }
+    // grad du = (sum_i du_i (x) dN_i/dxi) J^-1
+    float Gu[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) Gu[k] = 0.f;
+#pragma unroll
+    for (int i = 0; i < NPE; i++)
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) Gu[3 * a + j] = fmaf(du[i][a], G[i][j], Gu[3 * a + j]);
+    float L[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++)
+        L[3 * a + b] = Gu[3 * a + 0] * Ji[0 * 3 + b] + Gu[3 * a + 1] * Ji[1 * 3 + b] +
+                       Gu[3 * a + 2] * Ji[2 * 3 + b];
+    const float de[6] = {L[0], L[4], L[8], L[1] + L[3], L[5] + L[7], L[2] + L[6]};
+    const float tr = de[0] + de[1] + de[2];
+    float s[6];
+    if (MODE == EM_REFCOMPAT) {
+      s[0] = p.lambda * tr + 2.f * p.mu * de[0];
+      s[1] = p.lambda * tr + 2.f * p.mu * de[1];
+      s[2] = p.lambda * tr + 2.f * p.mu * de[2];
+      s[3] = p.mu * de[3];
+      s[4] = p.mu * de[4];
+      s[5] = p.mu * de[5];
+      if (p.accum_energy) {
+        float w = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; k++) w = fmaf(s[k], de[k], w);
+        wint = fmaf(0.5f * wd, w, wint);
+      }
+    } else {
+      const size_t qi = (size_t)q * E + e;
+      const float4 sa = S.sig_a[qi];
+      const float2 sb = S.sig_b[qi];
+      float ep = S.epbar[qi];
+      const float s0[6] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y};
+      s[0] = s0[0] + p.lambda * tr + 2.f * p.mu * de[0];
+      s[1] = s0[1] + p.lambda * tr + 2.f * p.mu * de[1];
+      s[2] = s0[2] + p.lambda * tr + 2.f * p.mu * de[2];
+      s[3] = s0[3] + p.mu * de[3];
+      s[4] = s0[4] + p.mu * de[4];
+      s[5] = s0[5] + p.mu * de[5];
+      const float ep0 = ep;
+      j2_return(p, s, ep);
+      S.sig_a[qi] = make_float4(s[0], s[1], s[2], s[3]);
+      S.sig_b[qi] = make_float2(s[4], s[5]);
+      S.epbar[qi] = ep;
+      if (p.accum_energy) {
+        float w = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; k++) w = fmaf(s0[k] + s[k], de[k], w);
+        wint = fmaf(0.5f * wd, w, wint);
+        wp = fmaf(wd * (p.sy0 + p.H * ep), ep - ep0, wp);
+      }
+    }
+    // f_i += wd sigma . dN_i/dx = sum_j P[a][j] dN_i/dxi_j with P = wd sigma J^-T
+    const float Sg[9] = {s[0], s[3], s[5], s[3], s[1], s[4], s[5], s[4], s[2]};
+    float Pm[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        Pm[3 * a + j] = wd * (Sg[3 * a + 0] * Ji[3 * j + 0] + Sg[3 * a + 1] * Ji[3 * j + 1] +
+                              Sg[3 * a + 2] * Ji[3 * j + 2]);
+#pragma unroll
+    for (int i = 0; i < NPE; i++)
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) f[i][a] = fmaf(Pm[3 * a + j], G[i][j], f[i][a]);
+  }
+  if (MODE == EM_MASS_HRZ && NPE == 10) {
+    // HRZ for the straight-sided tet10: rho V/36 at corners, 4 rho V/27 at edges.
+    const float mv = p.rho * vol;
+#pragma unroll
+    for (int i = 0; i < NPE; i++) f[i][0] = i < 4 ? mv * (1.f / 36.f) : mv * (4.f / 27.f);
+  }
+}
+
+template <int BS>
+__device__ __forceinline__ float block_sum(float v, float* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  float t = 0.f;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < BS / 32; k++) t += red[k];
+  return t;  // valid on thread 0
+}
+
+// K1 / K3.  Shared memory: x[3][Lmax] du[3][Lmax] acc[3][Lmax] floats + reduction.
+template <int NPE, int MODE, int BS>
+__global__ void __launch_bounds__(BS) k_elem(DevPlan P, DevState S, ElemParams p) {
+  extern __shared__ float sm[];
+  const ChunkInfo ch = P.chunks[blockIdx.x];
+  const int L = ch.n_local;
+  float* sx = sm;
+  float* sd = sm + 3 * L;
+  float* sa = sm + 6 * L;
+  __shared__ float red[BS / 32];
+  constexpr bool kMass = MODE == EM_MASS_ROWSUM || MODE == EM_MASS_HRZ;
+
+  for (int l = threadIdx.x; l < L; l += BS) {
+    const int lb = ch.local_begin + l;
+    const int g = P.local_gid[lb];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      sx[k * L + l] = P.local_x0[(size_t)k * P.Lt + lb] + (float)S.u[k][g];
+      sd[k * L + l] = kMass ? 0.f : p.dt * (float)S.v[k][g];
+      sa[k * L + l] = 0.f;
+    }
+  }
+  __syncthreads();
+
+  float wint = 0.f, wp = 0.f, vol = 0.f;
+  const int E = P.E;
+  for (int w = ch.elem_begin; w < ch.elem_end; w += BS) {
+    const int e = w + threadIdx.x;
+    const bool act = e < ch.elem_end;
+    int col = -1;
+    int ln[NPE];
+    float f[NPE][3];
+    if (act) {
+      col = P.color[e];
+      float x[NPE][3], du[NPE][3];
+#pragma unroll
+      for (int a = 0; a < NPE; a++) {
+        ln[a] = P.conn_local[(size_t)a * E + e];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          x[a][k] = sx[k * L + ln[a]];
+          du[a][k] = sd[k * L + ln[a]];
+        }
+      }
+      element_force<NPE, MODE>(p, S, e, E, x, du, f, wint, wp, vol);
+    }
+    const int c0 = P.color[w];
+    const int c1 = P.color[min(w + BS, ch.elem_end) - 1];
+    for (int k = c0; k <= c1; k++) {
+      __syncthreads();
+      if (col == k) {
+#pragma unroll
+        for (int a = 0; a < NPE; a++) {
+          sa[ln[a]] += f[a][0];
+          if (!kMass) {
+            sa[L + ln[a]] += f[a][1];
+            sa[2 * L + ln[a]] += f[a][2];
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int l = threadIdx.x; l < L; l += BS) {
+    const int s = P.local_slot[ch.local_begin + l];
+    S.slot_f[0][s] = sa[l];
+    if (!kMass) {
+      S.slot_f[1][s] = sa[L + l];
+      S.slot_f[2][s] = sa[2 * L + l];
+    }
+  }
+  if (p.accum_energy) {
+    const float t0 = block_sum<BS>(wint, red);
+    const float t1 = block_sum<BS>(wp, red);
+    const float t2 = block_sum<BS>(vol, red);
+    if (threadIdx.x == 0) {
+      double* cw = S.chunk_work + 4 * (size_t)blockIdx.x;
+      cw[0] += (double)t0;
+      cw[1] += (double)t1;
+      cw[2] += (double)t2;
+    }
+  }
+}
+
+// K2: node update.  INIT: a0 from zero internal force and v += dt/2 a0
+// (include/dynamics.h:454-463); otherwise one full central-difference step.
+template <bool INIT, bool STORE_ACC>
+__global__ void __launch_bounds__(256) k_node(NodeArrays A, NodeParams p) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= p.N) return;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  if (!INIT) {
+    const int s1 = A.slot_row[n + 1];
+    for (int s = A.slot_row[n]; s < s1; s++) {
+      fx += A.slot_f[0][s];
+      fy += A.slot_f[1][s];
+      fz += A.slot_f[2][s];
+    }
+  }
+  const float m = A.mass[n];
+  const float rm = 1.0f / m;
+  double a[3] = {(double)(-fx * rm) + p.g[0], (double)(-fy * rm) + p.g[1],
+                 (double)(-fz * rm) + p.g[2]};
+  double u[3], v[3], un[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    u[k] = A.u[k][n];
+    v[k] = A.v[k][n];
+    un[k] = INIT ? u[k] : fma(p.dt, v[k], u[k]);  // u + du, du = dt v
+  }
+  // wall at the end-of-step position (Wall::detect_contact on x + du)
+  const double d = A.d0[n] + p.wall_n[0] * un[0] + p.wall_n[1] * un[1] + p.wall_n[2] * un[2];
+  const unsigned char old = A.contact[n];
+  unsigned char flag = old & 2;
+  if (d < 0.0) {
+    const double c = -d * p.wall_k / (double)m;
+#pragma unroll
+    for (int k = 0; k < 3; k++) a[k] = fma(c, p.wall_n[k], a[k]);
+    flag = 3;
+  }
+  if (flag != old) A.contact[n] = flag;
+  const double h = INIT ? 0.5 * p.dt : p.dt;
+  bool finite = true;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double vn = fma(h, a[k], v[k]);
+    finite = finite && isfinite(vn);
+    A.v[k][n] = vn;
+    if (!INIT) A.u[k][n] = un[k];
+    if (STORE_ACC) A.acc[k][n] = (float)a[k];
+  }
+  if (!finite) atomicOr(A.status, (unsigned)ST_NONFINITE);
+}
+
+// Lumped mass: sum of the node's slots (component 0) in chunk order.
+__global__ void k_mass_sum(const float* slot_m, const int* slot_row, float* mass, int N) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float m = 0.f;
+  for (int s = slot_row[n]; s < slot_row[n + 1]; s++) m += slot_m[s];
+  mass[n] = m;
+}
+
+// Assembled internal force of a one-shot call: slot sums to FP64 [3][N].
+__global__ void k_force_sum(const float* sx, const float* sy, const float* sz, const int* slot_row,
+                            double* f, int N) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float a = 0.f, b = 0.f, c = 0.f;
+  for (int s = slot_row[n]; s < slot_row[n + 1]; s++) {
+    a += sx[s];
+    b += sy[s];
+    c += sz[s];
+  }
+  f[n] = a;
+  f[N + n] = b;
+  f[2 * (size_t)N + n] = c;
+}
+
+// Energy terms at the current state, one FP64 partial per block (fixed-order sums):
+// out[blk][0] kinetic (v_n = v - dt/2 a), [1] contact potential, [2] gravity work.
+__global__ void k_energy(NodeArrays A, NodeParams p, double* out) {
+  __shared__ double red[3][256];
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  double ke = 0.0, phi = 0.0, wg = 0.0;
+  if (n < p.N) {
+    const double m = A.mass[n];
+    double v2 = 0.0;
+    for (int k = 0; k < 3; k++) {
+      const double vn = A.v[k][n] - 0.5 * p.dt * (double)A.acc[k][n];
+      v2 += vn * vn;
+      wg += m * p.g[k] * A.u[k][n];
+    }
+    ke = 0.5 * m * v2;
+    const double d = A.d0[n] + p.wall_n[0] * A.u[0][n] + p.wall_n[1] * A.u[1][n] +
+                     p.wall_n[2] * A.u[2][n];
+    if (d < 0.0) phi = 0.5 * p.wall_k * d * d;
+  }
+  red[0][threadIdx.x] = ke;
+  red[1][threadIdx.x] = phi;
+  red[2][threadIdx.x] = wg;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 3; k++) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 3; k++) out[3 * (size_t)blockIdx.x + k] = red[k][0];
+}
+
+}  // namespace ci

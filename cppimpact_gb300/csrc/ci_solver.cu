@@ -1,0 +1,890 @@
+// ci_solver.cu -- C ABI of the GB300 impact step (declared in include/cppimpact_gb300.h).
+//
+// Host orchestration: preprocessing (ci_plan.cpp), device buffers, the one-time
+// lumped mass and initial half step, graph-captured stepping, read-back in the
+// caller's node/element order, one-shot kernels for parity checks.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/cppimpact_gb300.h"
+#include "ci_kernels.cuh"
+#include "ci_plan.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define CI_CUDA(call)                                                                      \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(CI_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),     \
+                  __FILE__, __LINE__);                                                     \
+  } while (0)
+
+constexpr int kBS = 256;
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t alloc(size_t count) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(&p, sizeof(T) * count);
+  }
+};
+
+}  // namespace
+
+struct ci_solver {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  ci::Plan plan;
+  int N = 0, E = 0, npe = 0, nq = 0, C = 0;
+  long long S = 0, Lt = 0;
+  ci_material mat{};
+  ci_wall wall{};
+  ci_options opt{};
+  std::vector<double> X0;   // mesh positions, caller order [3N]
+  std::vector<double> X;    // reference positions X0 + pos, caller order
+  std::vector<double> vel0; // initial velocity
+  double dt = 0.0;
+  bool started = false;
+  long long steps_done = 0;
+  size_t smem_bytes = 0;
+
+  // device plan
+  DBuf<ci::ChunkInfo> d_chunks;
+  DBuf<uint16_t> d_conn;
+  DBuf<uint8_t> d_color;
+  DBuf<int> d_lgid, d_lslot, d_slot_row;
+  DBuf<float> d_lx0;  // [3][Lt]
+  // state
+  DBuf<double> d_u, d_v;   // [3][N]
+  DBuf<float> d_slot;      // [3][S]
+  DBuf<float> d_mass;      // [N]
+  DBuf<double> d_d0;       // [N]
+  DBuf<unsigned char> d_contact;
+  DBuf<float> d_acc;       // [3][N]
+  DBuf<float4> d_sig_a;
+  DBuf<float2> d_sig_b;
+  DBuf<float> d_epbar;
+  DBuf<double> d_work;     // [C][4]
+  DBuf<unsigned int> d_status;
+  // one-shot scratch (never aliases the running state)
+  DBuf<double> d_u2, d_v2, d_f;
+  DBuf<float4> d_sig_a2;
+  DBuf<float2> d_sig_b2;
+  DBuf<float> d_epbar2;
+  DBuf<double> d_epart;
+
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+
+  ci::DevPlan dev_plan() const {
+    ci::DevPlan P;
+    P.chunks = d_chunks.p;
+    P.conn_local = d_conn.p;
+    P.color = d_color.p;
+    P.local_gid = d_lgid.p;
+    P.local_slot = d_lslot.p;
+    P.local_x0 = d_lx0.p;
+    P.slot_row = d_slot_row.p;
+    P.E = E;
+    P.N = N;
+    P.Lt = (int)Lt;
+    return P;
+  }
+  ci::DevState dev_state(double* u, double* v) const {
+    ci::DevState D;
+    for (int k = 0; k < 3; k++) {
+      D.u[k] = u + (size_t)k * N;
+      D.v[k] = v + (size_t)k * N;
+      D.slot_f[k] = d_slot.p + (size_t)k * S;
+    }
+    D.sig_a = d_sig_a.p;
+    D.sig_b = d_sig_b.p;
+    D.epbar = d_epbar.p;
+    D.chunk_work = d_work.p;
+    D.status = d_status.p;
+    return D;
+  }
+  ci::ElemParams elem_params(float dtf, bool energy) const {
+    ci::ElemParams p;
+    p.dt = dtf;
+    p.mu = (float)(mat.E / (2.0 * (1.0 + mat.nu)));
+    p.lambda = (float)(mat.E * mat.nu / ((1.0 + mat.nu) * (1.0 - 2.0 * mat.nu)));
+    const bool elastic = !(mat.sigma_y0 > 0.0) || mat.sigma_y0 > 1e30;
+    p.sy0 = elastic ? 3.0e38f : (float)mat.sigma_y0;
+    p.H = (float)mat.H;
+    p.rho = (float)mat.rho;
+    p.accum_energy = energy ? 1 : 0;
+    return p;
+  }
+  ci::NodeArrays node_arrays() const {
+    ci::NodeArrays A;
+    for (int k = 0; k < 3; k++) {
+      A.u[k] = d_u.p + (size_t)k * N;
+      A.v[k] = d_v.p + (size_t)k * N;
+      A.slot_f[k] = d_slot.p + (size_t)k * S;
+      A.acc[k] = d_acc.p + (size_t)k * N;
+    }
+    A.slot_row = d_slot_row.p;
+    A.mass = d_mass.p;
+    A.d0 = d_d0.p;
+    A.contact = d_contact.p;
+    A.status = d_status.p;
+    return A;
+  }
+  ci::NodeParams node_params() const {
+    ci::NodeParams p;
+    p.dt = dt;
+    for (int k = 0; k < 3; k++) {
+      p.g[k] = opt.gravity[k];
+      p.wall_n[k] = wall.normal[k];
+    }
+    p.wall_k = wall.stiffness;
+    p.N = N;
+    return p;
+  }
+};
+
+namespace {
+
+template <int NPE, int MODE>
+cudaError_t launch_elem(ci_solver* s, const ci::DevState& D, const ci::ElemParams& p) {
+  ci::k_elem<NPE, MODE, kBS><<<s->C, kBS, s->smem_bytes, s->stream>>>(s->dev_plan(), D, p);
+  return cudaGetLastError();
+}
+
+// Raise the dynamic shared-memory limit of the element kernels once per solver (not
+// inside stream capture).
+template <int NPE>
+cudaError_t configure_npe(int bytes) {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(ci::k_elem<NPE, ci::EM_J2, kBS>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+    return e;
+  if ((e = cudaFuncSetAttribute(ci::k_elem<NPE, ci::EM_REFCOMPAT, kBS>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+    return e;
+  if ((e = cudaFuncSetAttribute(ci::k_elem<NPE, ci::EM_MASS_ROWSUM, kBS>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+    return e;
+  return cudaFuncSetAttribute(ci::k_elem<NPE, ci::EM_MASS_HRZ, kBS>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+cudaError_t launch_elem_mode(ci_solver* s, int mode, const ci::DevState& D, const ci::ElemParams& p) {
+  if (s->npe == 4) {
+    switch (mode) {
+      case ci::EM_J2: return launch_elem<4, ci::EM_J2>(s, D, p);
+      case ci::EM_REFCOMPAT: return launch_elem<4, ci::EM_REFCOMPAT>(s, D, p);
+      case ci::EM_MASS_ROWSUM: return launch_elem<4, ci::EM_MASS_ROWSUM>(s, D, p);
+      default: return launch_elem<4, ci::EM_MASS_HRZ>(s, D, p);
+    }
+  }
+  switch (mode) {
+    case ci::EM_J2: return launch_elem<10, ci::EM_J2>(s, D, p);
+    case ci::EM_REFCOMPAT: return launch_elem<10, ci::EM_REFCOMPAT>(s, D, p);
+    case ci::EM_MASS_ROWSUM: return launch_elem<10, ci::EM_MASS_ROWSUM>(s, D, p);
+    default: return launch_elem<10, ci::EM_MASS_HRZ>(s, D, p);
+  }
+}
+
+int step_mode(const ci_solver* s) {
+  return s->opt.mode == CI_MODE_REFCOMPAT ? ci::EM_REFCOMPAT : ci::EM_J2;
+}
+
+// One time step: K1 then K2.
+cudaError_t enqueue_step(ci_solver* s, bool store_acc) {
+  const ci::DevState D = s->dev_state(s->d_u.p, s->d_v.p);
+  cudaError_t e = launch_elem_mode(s, step_mode(s), D, s->elem_params((float)s->dt, true));
+  if (e != cudaSuccess) return e;
+  const int nb = (s->N + 255) / 256;
+  if (store_acc)
+    ci::k_node<false, true><<<nb, 256, 0, s->stream>>>(s->node_arrays(), s->node_params());
+  else
+    ci::k_node<false, false><<<nb, 256, 0, s->stream>>>(s->node_arrays(), s->node_params());
+  return cudaGetLastError();
+}
+
+int check_status(ci_solver* s) {
+  unsigned int st = 0;
+  CI_CUDA(cudaMemcpyAsync(&st, s->d_status.p, sizeof(st), cudaMemcpyDeviceToHost, s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  if (st & ci::ST_DEGENERATE) return fail(CI_ERR_DEGENERATE, "an element has det J <= 0");
+  if (st & ci::ST_NONFINITE) return fail(CI_ERR_NONFINITE, "non-finite nodal state");
+  return CI_OK;
+}
+
+// Per-chunk reference coordinates relative to the chunk origin (first owned node, or
+// the first local node), and the wall offsets d0 = n . X - offset, in plan order.
+int upload_reference(ci_solver* s) {
+  const ci::Plan& P = s->plan;
+  std::vector<float> lx0(3 * (size_t)s->Lt);
+  for (int c = 0; c < s->C; c++) {
+    const ci::ChunkInfo& ch = P.chunks[c];
+    const int o = P.node_orig[P.local_gid[ch.local_begin]];
+    for (int l = 0; l < ch.n_local; l++) {
+      const int lb = ch.local_begin + l;
+      const int n = P.node_orig[P.local_gid[lb]];
+      for (int k = 0; k < 3; k++)
+        lx0[(size_t)k * s->Lt + lb] = (float)(s->X[3 * (size_t)n + k] - s->X[3 * (size_t)o + k]);
+    }
+  }
+  std::vector<double> d0(s->N);
+  for (int i = 0; i < s->N; i++) {
+    const int n = P.node_orig[i];
+    d0[i] = s->wall.normal[0] * s->X[3 * (size_t)n] + s->wall.normal[1] * s->X[3 * (size_t)n + 1] +
+            s->wall.normal[2] * s->X[3 * (size_t)n + 2] - s->wall.offset;
+  }
+  CI_CUDA(cudaMemcpyAsync(s->d_lx0.p, lx0.data(), sizeof(float) * lx0.size(),
+                          cudaMemcpyHostToDevice, s->stream));
+  CI_CUDA(cudaMemcpyAsync(s->d_d0.p, d0.data(), sizeof(double) * d0.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  return CI_OK;
+}
+
+int reset_state(ci_solver* s) {
+  const int N = s->N;
+  std::vector<double> v(3 * (size_t)N);
+  for (int i = 0; i < N; i++)
+    for (int k = 0; k < 3; k++) v[(size_t)k * N + i] = s->vel0[k];
+  CI_CUDA(cudaMemsetAsync(s->d_u.p, 0, sizeof(double) * 3 * N, s->stream));
+  CI_CUDA(cudaMemcpyAsync(s->d_v.p, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  if (s->d_sig_a.p) {
+    CI_CUDA(cudaMemsetAsync(s->d_sig_a.p, 0, sizeof(float4) * s->d_sig_a.n, s->stream));
+    CI_CUDA(cudaMemsetAsync(s->d_sig_b.p, 0, sizeof(float2) * s->d_sig_b.n, s->stream));
+    CI_CUDA(cudaMemsetAsync(s->d_epbar.p, 0, sizeof(float) * s->d_epbar.n, s->stream));
+  }
+  CI_CUDA(cudaMemsetAsync(s->d_contact.p, 0, N, s->stream));
+  CI_CUDA(cudaMemsetAsync(s->d_acc.p, 0, sizeof(float) * 3 * N, s->stream));
+  CI_CUDA(cudaMemsetAsync(s->d_work.p, 0, sizeof(double) * 4 * s->C, s->stream));
+  CI_CUDA(cudaMemsetAsync(s->d_status.p, 0, sizeof(unsigned int), s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  s->started = false;
+  s->steps_done = 0;
+  return CI_OK;
+}
+
+int compute_mass(ci_solver* s) {
+  const ci::DevState D = s->dev_state(s->d_u.p, s->d_v.p);
+  const int mode = s->opt.lumping == CI_LUMP_HRZ ? ci::EM_MASS_HRZ : ci::EM_MASS_ROWSUM;
+  CI_CUDA(launch_elem_mode(s, mode, D, s->elem_params(0.f, false)));
+  ci::k_mass_sum<<<(s->N + 255) / 256, 256, 0, s->stream>>>(s->d_slot.p, s->d_slot_row.p,
+                                                            s->d_mass.p, s->N);
+  CI_CUDA(cudaGetLastError());
+  return CI_OK;
+}
+
+void destroy_graph(ci_solver* s) {
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
+  s->graph_steps = 0;
+}
+
+int build_graph(ci_solver* s, int steps) {
+  destroy_graph(s);
+  cudaGraph_t g = nullptr;
+  CI_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t err = cudaSuccess;
+  for (int i = 0; i < steps && err == cudaSuccess; i++) err = enqueue_step(s, false);
+  cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+  if (err != cudaSuccess) return fail(CI_ERR_CUDA, "graph capture: %s", cudaGetErrorString(err));
+  if (e2 != cudaSuccess) return fail(CI_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e2));
+  err = cudaGraphInstantiate(&s->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (err != cudaSuccess) return fail(CI_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(err));
+  s->graph_steps = steps;
+  return CI_OK;
+}
+
+// Enqueue n steps; the last stores the acceleration for energy read-back.
+int enqueue_steps(ci_solver* s, int n) {
+  if (n <= 0) return CI_OK;
+  const int G = s->opt.graph_steps > 0 ? s->opt.graph_steps : 32;
+  int rest = n - 1;
+  if (rest >= G) {
+    if (!s->graph || s->graph_steps != G) {
+      const int rc = build_graph(s, G);
+      if (rc) return rc;
+    }
+    while (rest >= G) {
+      CI_CUDA(cudaGraphLaunch(s->graph, s->stream));
+      rest -= G;
+    }
+  }
+  for (; rest > 0; rest--) CI_CUDA(enqueue_step(s, false));
+  CI_CUDA(enqueue_step(s, true));
+  s->steps_done += n;
+  return CI_OK;
+}
+
+int require_started(ci_solver* s) {
+  if (!s) return fail(CI_ERR_INVALID, "null solver");
+  if (!s->started) return fail(CI_ERR_INVALID, "call ci_start or ci_solve before stepping");
+  return CI_OK;
+}
+
+template <typename T>
+int upload(DBuf<T>& b, const std::vector<T>& h, cudaStream_t st) {
+  CI_CUDA(b.alloc(h.size()));
+  if (!h.empty())
+    CI_CUDA(cudaMemcpyAsync(b.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, st));
+  return CI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ci_abi_version(void) { return CI_ABI_VERSION; }
+
+const char* ci_last_error(void) { return g_last_error.c_str(); }
+
+void ci_default_options(ci_options* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->mode = CI_MODE_J2;
+  o->lumping = CI_LUMP_HRZ;
+  o->gravity[2] = -9.81;
+}
+
+int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
+              const ci_options* opt, ci_solver** out) {
+  if (!mesh || !mat || !wall || !out) return fail(CI_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (mesh->nodes_per_element != 4 && mesh->nodes_per_element != 10)
+    return fail(CI_ERR_UNSUPPORTED, "nodes_per_element must be 4 or 10");
+  if (!mesh->xloc || !mesh->element_nodes || mesh->num_nodes <= 0 || mesh->num_elements <= 0)
+    return fail(CI_ERR_INVALID, "empty mesh");
+  if (mat->beta != 0.0) return fail(CI_ERR_UNSUPPORTED, "only isotropic hardening (beta = 0)");
+  if (!(mat->E > 0.0) || !(mat->rho > 0.0) || !(mat->nu > -1.0 && mat->nu < 0.5))
+    return fail(CI_ERR_INVALID, "material needs E > 0, rho > 0, -1 < nu < 0.5");
+  std::unique_ptr<ci_solver> s(new ci_solver());
+  if (opt)
+    s->opt = *opt;
+  else
+    ci_default_options(&s->opt);
+  if (s->opt.mode != CI_MODE_J2 && s->opt.mode != CI_MODE_REFCOMPAT)
+    return fail(CI_ERR_INVALID, "unknown mode");
+  s->mat = *mat;
+  s->wall = *wall;
+  s->N = mesh->num_nodes;
+  s->E = mesh->num_elements;
+  s->npe = mesh->nodes_per_element;
+  s->nq = s->npe == 4 ? 1 : 4;
+  s->device = s->opt.device;
+  CI_CUDA(cudaSetDevice(s->device));
+  int sms = 0;
+  CI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+  std::string err;
+  if (!ci::build_plan(s->N, s->E, s->npe, mesh->xloc, mesh->element_nodes, s->opt.chunk_elements,
+                      s->opt.chunk_nodes, 2 * sms, &s->plan, &err))
+    return fail(CI_ERR_INVALID, "%s", err.c_str());
+  const ci::Plan& P = s->plan;
+  s->C = P.n_chunks;
+  s->S = P.slot_row[s->N];
+  s->Lt = (long long)P.local_gid.size();
+  s->smem_bytes = sizeof(float) * 9 * (size_t)P.max_local;
+  int smem_max = 0;
+  CI_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
+  if ((long long)s->smem_bytes + 1024 > smem_max)
+    return fail(CI_ERR_TOO_LARGE, "chunk needs %zu B of shared memory", s->smem_bytes);
+  s->X0.assign(mesh->xloc, mesh->xloc + 3 * (size_t)s->N);
+  s->X = s->X0;
+  s->vel0.assign(3, 0.0);
+
+  CI_CUDA(s->npe == 4 ? configure_npe<4>((int)s->smem_bytes) : configure_npe<10>((int)s->smem_bytes));
+  CI_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  CI_CUDA(cudaEventCreate(&s->ev0));
+  CI_CUDA(cudaEventCreate(&s->ev1));
+  int rc;
+  if ((rc = upload(s->d_chunks, P.chunks, s->stream))) return rc;
+  if ((rc = upload(s->d_conn, P.conn_local, s->stream))) return rc;
+  if ((rc = upload(s->d_color, P.color, s->stream))) return rc;
+  if ((rc = upload(s->d_lgid, P.local_gid, s->stream))) return rc;
+  if ((rc = upload(s->d_lslot, P.local_slot, s->stream))) return rc;
+  if ((rc = upload(s->d_slot_row, P.slot_row, s->stream))) return rc;
+  const size_t N = s->N, E = s->E;
+  CI_CUDA(s->d_lx0.alloc(3 * (size_t)s->Lt));
+  CI_CUDA(s->d_u.alloc(3 * N));
+  CI_CUDA(s->d_v.alloc(3 * N));
+  CI_CUDA(s->d_slot.alloc(3 * (size_t)s->S));
+  CI_CUDA(s->d_mass.alloc(N));
+  CI_CUDA(s->d_d0.alloc(N));
+  CI_CUDA(s->d_contact.alloc(N));
+  CI_CUDA(s->d_acc.alloc(3 * N));
+  CI_CUDA(s->d_sig_a.alloc(E * s->nq));
+  CI_CUDA(s->d_sig_b.alloc(E * s->nq));
+  CI_CUDA(s->d_epbar.alloc(E * s->nq));
+  CI_CUDA(s->d_work.alloc(4 * (size_t)s->C));
+  CI_CUDA(s->d_status.alloc(1));
+  CI_CUDA(s->d_epart.alloc(3 * ((N + 255) / 256)));
+  if ((rc = upload_reference(s.get()))) return rc;
+  if ((rc = reset_state(s.get()))) return rc;
+  *out = s.release();
+  return CI_OK;
+}
+
+int ci_destroy(ci_solver* s) {
+  if (!s) return CI_OK;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  destroy_graph(s);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  cudaStream_t st = s->stream;
+  delete s;
+  if (st) cudaStreamDestroy(st);
+  return CI_OK;
+}
+
+int ci_initialize(ci_solver* s, const double pos[3], const double vel[3]) {
+  if (!s || !pos || !vel) return fail(CI_ERR_INVALID, "null argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  for (int i = 0; i < s->N; i++)
+    for (int k = 0; k < 3; k++) s->X[3 * (size_t)i + k] = s->X0[3 * (size_t)i + k] + pos[k];
+  for (int k = 0; k < 3; k++) s->vel0[k] = vel[k];
+  int rc = upload_reference(s);
+  if (rc) return rc;
+  return reset_state(s);
+}
+
+int ci_start(ci_solver* s, double dt) {
+  if (!s) return fail(CI_ERR_INVALID, "null solver");
+  if (!(dt > 0.0)) return fail(CI_ERR_INVALID, "dt must be positive");
+  CI_CUDA(cudaSetDevice(s->device));
+  int rc = reset_state(s);
+  if (rc) return rc;
+  s->dt = dt;
+  destroy_graph(s);
+  if ((rc = compute_mass(s))) return rc;
+  ci::k_node<true, true><<<(s->N + 255) / 256, 256, 0, s->stream>>>(s->node_arrays(),
+                                                                    s->node_params());
+  CI_CUDA(cudaGetLastError());
+  s->started = true;
+  return check_status(s);
+}
+
+int ci_step(ci_solver* s, int nsteps) {
+  int rc = require_started(s);
+  if (rc) return rc;
+  if (nsteps < 0) return fail(CI_ERR_INVALID, "nsteps < 0");
+  CI_CUDA(cudaSetDevice(s->device));
+  if ((rc = enqueue_steps(s, nsteps))) return rc;
+  return check_status(s);
+}
+
+int ci_solve(ci_solver* s, double dt, double time_end, int export_interval) {
+  (void)export_interval;
+  int rc = ci_start(s, dt);
+  if (rc) return rc;
+  long long n = 0;
+  for (double t = 0.0; t <= time_end; t += dt) n++;  // the reference's loop count
+  while (n > 0) {
+    const int chunk = (int)std::min<long long>(n, 1 << 20);
+    if ((rc = ci_step(s, chunk))) return rc;
+    n -= chunk;
+  }
+  return CI_OK;
+}
+
+int ci_steps_done(const ci_solver* s, long long* nsteps) {
+  if (!s || !nsteps) return fail(CI_ERR_INVALID, "null argument");
+  *nsteps = s->steps_done;
+  return CI_OK;
+}
+
+int ci_get_state(ci_solver* s, double* x, double* v, double* mass, float* sigma, float* epbar,
+                 unsigned char* contact) {
+  if (!s) return fail(CI_ERR_INVALID, "null solver");
+  CI_CUDA(cudaSetDevice(s->device));
+  const int N = s->N, E = s->E, nq = s->nq;
+  const ci::Plan& P = s->plan;
+  std::vector<double> hu, hv;
+  if (x || v) {
+    hu.resize(3 * (size_t)N);
+    hv.resize(3 * (size_t)N);
+    CI_CUDA(cudaMemcpyAsync(hu.data(), s->d_u.p, sizeof(double) * hu.size(), cudaMemcpyDeviceToHost,
+                            s->stream));
+    CI_CUDA(cudaMemcpyAsync(hv.data(), s->d_v.p, sizeof(double) * hv.size(), cudaMemcpyDeviceToHost,
+                            s->stream));
+  }
+  std::vector<float> hm, hep;
+  std::vector<float4> hsa;
+  std::vector<float2> hsb;
+  std::vector<unsigned char> hc;
+  if (mass) {
+    hm.resize(N);
+    CI_CUDA(cudaMemcpyAsync(hm.data(), s->d_mass.p, sizeof(float) * N, cudaMemcpyDeviceToHost,
+                            s->stream));
+  }
+  if (sigma) {
+    hsa.resize((size_t)E * nq);
+    hsb.resize((size_t)E * nq);
+    CI_CUDA(cudaMemcpyAsync(hsa.data(), s->d_sig_a.p, sizeof(float4) * hsa.size(),
+                            cudaMemcpyDeviceToHost, s->stream));
+    CI_CUDA(cudaMemcpyAsync(hsb.data(), s->d_sig_b.p, sizeof(float2) * hsb.size(),
+                            cudaMemcpyDeviceToHost, s->stream));
+  }
+  if (epbar) {
+    hep.resize((size_t)E * nq);
+    CI_CUDA(cudaMemcpyAsync(hep.data(), s->d_epbar.p, sizeof(float) * hep.size(),
+                            cudaMemcpyDeviceToHost, s->stream));
+  }
+  if (contact) {
+    hc.resize(N);
+    CI_CUDA(cudaMemcpyAsync(hc.data(), s->d_contact.p, N, cudaMemcpyDeviceToHost, s->stream));
+  }
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  for (int i = 0; i < N; i++) {
+    const int n = P.node_orig[i];
+    for (int k = 0; k < 3; k++) {
+      if (x) x[3 * (size_t)n + k] = s->X[3 * (size_t)n + k] + hu[(size_t)k * N + i];
+      if (v) v[3 * (size_t)n + k] = hv[(size_t)k * N + i];
+    }
+    if (mass) mass[n] = hm[i];
+    if (contact) contact[n] = hc[i];
+  }
+  for (int pe = 0; pe < E; pe++) {
+    const int oe = P.elem_orig[pe];
+    for (int q = 0; q < nq; q++) {
+      const size_t qi = (size_t)q * E + pe, o = (size_t)oe * nq + q;
+      if (sigma) {
+        const float4 a = hsa[qi];
+        const float2 b = hsb[qi];
+        float* d = sigma + 6 * o;
+        d[0] = a.x; d[1] = a.y; d[2] = a.z; d[3] = a.w; d[4] = b.x; d[5] = b.y;
+      }
+      if (epbar) epbar[o] = hep[qi];
+    }
+  }
+  return CI_OK;
+}
+
+int ci_set_state(ci_solver* s, const double* x, const double* v) {
+  if (!s || !x || !v) return fail(CI_ERR_INVALID, "null argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  const int N = s->N;
+  const ci::Plan& P = s->plan;
+  std::vector<double> hu(3 * (size_t)N), hv(3 * (size_t)N);
+  for (int i = 0; i < N; i++) {
+    const int n = P.node_orig[i];
+    for (int k = 0; k < 3; k++) {
+      hu[(size_t)k * N + i] = x[3 * (size_t)n + k] - s->X[3 * (size_t)n + k];
+      hv[(size_t)k * N + i] = v[3 * (size_t)n + k];
+    }
+  }
+  CI_CUDA(cudaMemcpyAsync(s->d_u.p, hu.data(), sizeof(double) * hu.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  CI_CUDA(cudaMemcpyAsync(s->d_v.p, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  return CI_OK;
+}
+
+int ci_get_energy(ci_solver* s, ci_energy* e) {
+  if (!s || !e) return fail(CI_ERR_INVALID, "null argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  const int nb = (s->N + 255) / 256;
+  ci::k_energy<<<nb, 256, 0, s->stream>>>(s->node_arrays(), s->node_params(), s->d_epart.p);
+  CI_CUDA(cudaGetLastError());
+  std::vector<double> part(3 * (size_t)nb), work(4 * (size_t)s->C);
+  CI_CUDA(cudaMemcpyAsync(part.data(), s->d_epart.p, sizeof(double) * part.size(),
+                          cudaMemcpyDeviceToHost, s->stream));
+  CI_CUDA(cudaMemcpyAsync(work.data(), s->d_work.p, sizeof(double) * work.size(),
+                          cudaMemcpyDeviceToHost, s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  double ke = 0, phi = 0, wg = 0, wi = 0, wp = 0;
+  for (int b = 0; b < nb; b++) {
+    ke += part[3 * b];
+    phi += part[3 * b + 1];
+    wg += part[3 * b + 2];
+  }
+  for (int c = 0; c < s->C; c++) {
+    wi += work[4 * c];
+    wp += work[4 * c + 1];
+  }
+  // initial kinetic energy and contact potential from the reference state
+  double m_tot = 0.0, phi0 = 0.0;
+  std::vector<float> hm(s->N);
+  CI_CUDA(cudaMemcpy(hm.data(), s->d_mass.p, sizeof(float) * s->N, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < s->N; i++) {
+    m_tot += hm[i];
+    const int n = s->plan.node_orig[i];
+    const double d = s->wall.normal[0] * s->X[3 * (size_t)n] + s->wall.normal[1] * s->X[3 * (size_t)n + 1] +
+                     s->wall.normal[2] * s->X[3 * (size_t)n + 2] - s->wall.offset;
+    if (d < 0.0) phi0 += 0.5 * s->wall.stiffness * d * d;
+  }
+  const double v2 = s->vel0[0] * s->vel0[0] + s->vel0[1] * s->vel0[1] + s->vel0[2] * s->vel0[2];
+  e->kinetic = ke;
+  e->internal = wi;
+  e->plastic = wp;
+  e->contact = -(phi - phi0);
+  e->gravity = wg;
+  e->kinetic0 = 0.5 * m_tot * v2;
+  e->balance = ke + wi - e->contact - wg - e->kinetic0;
+  return CI_OK;
+}
+
+int ci_get_status(ci_solver* s, unsigned int* status) {
+  if (!s || !status) return fail(CI_ERR_INVALID, "null argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  CI_CUDA(cudaMemcpyAsync(status, s->d_status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                          s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  return CI_OK;
+}
+
+int ci_internal_force(ci_solver* s, const double* x, const double* du, const float* sigma_in,
+                      const float* epbar_in, double* f, float* sigma_out, float* epbar_out) {
+  if (!s || !x || !du || !f) return fail(CI_ERR_INVALID, "null argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  const int N = s->N, E = s->E, nq = s->nq;
+  const ci::Plan& P = s->plan;
+  std::vector<double> hu(3 * (size_t)N), hv(3 * (size_t)N);
+  for (int i = 0; i < N; i++) {
+    const int n = P.node_orig[i];
+    for (int k = 0; k < 3; k++) {
+      hu[(size_t)k * N + i] = x[3 * (size_t)n + k] - s->X[3 * (size_t)n + k];
+      hv[(size_t)k * N + i] = du[3 * (size_t)n + k];
+    }
+  }
+  CI_CUDA(s->d_u2.alloc(3 * (size_t)N));
+  CI_CUDA(s->d_v2.alloc(3 * (size_t)N));
+  CI_CUDA(s->d_f.alloc(3 * (size_t)N));
+  CI_CUDA(cudaMemcpyAsync(s->d_u2.p, hu.data(), sizeof(double) * hu.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  CI_CUDA(cudaMemcpyAsync(s->d_v2.p, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  const bool j2 = s->opt.mode == CI_MODE_J2;
+  if (j2) {
+    CI_CUDA(s->d_sig_a2.alloc((size_t)E * nq));
+    CI_CUDA(s->d_sig_b2.alloc((size_t)E * nq));
+    CI_CUDA(s->d_epbar2.alloc((size_t)E * nq));
+    std::vector<float4> sa((size_t)E * nq, make_float4(0, 0, 0, 0));
+    std::vector<float2> sb((size_t)E * nq, make_float2(0, 0));
+    std::vector<float> ep((size_t)E * nq, 0.f);
+    for (int pe = 0; pe < E; pe++)
+      for (int q = 0; q < nq; q++) {
+        const size_t qi = (size_t)q * E + pe, o = (size_t)P.elem_orig[pe] * nq + q;
+        if (sigma_in) {
+          const float* d = sigma_in + 6 * o;
+          sa[qi] = make_float4(d[0], d[1], d[2], d[3]);
+          sb[qi] = make_float2(d[4], d[5]);
+        }
+        if (epbar_in) ep[qi] = epbar_in[o];
+      }
+    CI_CUDA(cudaMemcpyAsync(s->d_sig_a2.p, sa.data(), sizeof(float4) * sa.size(),
+                            cudaMemcpyHostToDevice, s->stream));
+    CI_CUDA(cudaMemcpyAsync(s->d_sig_b2.p, sb.data(), sizeof(float2) * sb.size(),
+                            cudaMemcpyHostToDevice, s->stream));
+    CI_CUDA(cudaMemcpyAsync(s->d_epbar2.p, ep.data(), sizeof(float) * ep.size(),
+                            cudaMemcpyHostToDevice, s->stream));
+  }
+  ci::DevState D = s->dev_state(s->d_u2.p, s->d_v2.p);
+  D.sig_a = s->d_sig_a2.p;
+  D.sig_b = s->d_sig_b2.p;
+  D.epbar = s->d_epbar2.p;
+  CI_CUDA(launch_elem_mode(s, step_mode(s), D, s->elem_params(1.0f, false)));
+  ci::k_force_sum<<<(N + 255) / 256, 256, 0, s->stream>>>(
+      s->d_slot.p, s->d_slot.p + s->S, s->d_slot.p + 2 * s->S, s->d_slot_row.p, s->d_f.p, N);
+  CI_CUDA(cudaGetLastError());
+  std::vector<double> hf(3 * (size_t)N);
+  CI_CUDA(cudaMemcpyAsync(hf.data(), s->d_f.p, sizeof(double) * hf.size(), cudaMemcpyDeviceToHost,
+                          s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  for (int i = 0; i < N; i++)
+    for (int k = 0; k < 3; k++) f[3 * (size_t)P.node_orig[i] + k] = hf[(size_t)k * N + i];
+  if (j2 && (sigma_out || epbar_out)) {
+    std::vector<float4> sa((size_t)E * nq);
+    std::vector<float2> sb((size_t)E * nq);
+    std::vector<float> ep((size_t)E * nq);
+    CI_CUDA(cudaMemcpy(sa.data(), s->d_sig_a2.p, sizeof(float4) * sa.size(), cudaMemcpyDeviceToHost));
+    CI_CUDA(cudaMemcpy(sb.data(), s->d_sig_b2.p, sizeof(float2) * sb.size(), cudaMemcpyDeviceToHost));
+    CI_CUDA(cudaMemcpy(ep.data(), s->d_epbar2.p, sizeof(float) * ep.size(), cudaMemcpyDeviceToHost));
+    for (int pe = 0; pe < E; pe++)
+      for (int q = 0; q < nq; q++) {
+        const size_t qi = (size_t)q * E + pe, o = (size_t)P.elem_orig[pe] * nq + q;
+        if (sigma_out) {
+          float* d = sigma_out + 6 * o;
+          d[0] = sa[qi].x; d[1] = sa[qi].y; d[2] = sa[qi].z; d[3] = sa[qi].w;
+          d[4] = sb[qi].x; d[5] = sb[qi].y;
+        }
+        if (epbar_out) epbar_out[o] = ep[qi];
+      }
+  }
+  return check_status(s);
+}
+
+int ci_lumped_mass(ci_solver* s, const double* x, double* mass) {
+  if (!s || !x || !mass) return fail(CI_ERR_INVALID, "null argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  const int N = s->N;
+  const ci::Plan& P = s->plan;
+  std::vector<double> hu(3 * (size_t)N);
+  for (int i = 0; i < N; i++) {
+    const int n = P.node_orig[i];
+    for (int k = 0; k < 3; k++) hu[(size_t)k * N + i] = x[3 * (size_t)n + k] - s->X[3 * (size_t)n + k];
+  }
+  CI_CUDA(s->d_u2.alloc(3 * (size_t)N));
+  CI_CUDA(s->d_v2.alloc(3 * (size_t)N));
+  CI_CUDA(cudaMemcpyAsync(s->d_u2.p, hu.data(), sizeof(double) * hu.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  const ci::DevState D = s->dev_state(s->d_u2.p, s->d_v2.p);
+  const int mode = s->opt.lumping == CI_LUMP_HRZ ? ci::EM_MASS_HRZ : ci::EM_MASS_ROWSUM;
+  CI_CUDA(launch_elem_mode(s, mode, D, s->elem_params(0.f, false)));
+  DBuf<float> m;
+  CI_CUDA(m.alloc(N));
+  ci::k_mass_sum<<<(N + 255) / 256, 256, 0, s->stream>>>(s->d_slot.p, s->d_slot_row.p, m.p, N);
+  CI_CUDA(cudaGetLastError());
+  std::vector<float> hm(N);
+  CI_CUDA(cudaMemcpyAsync(hm.data(), m.p, sizeof(float) * N, cudaMemcpyDeviceToHost, s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  for (int i = 0; i < N; i++) mass[P.node_orig[i]] = hm[i];
+  return check_status(s);
+}
+
+int ci_strain_energy(ci_solver* s, const double* u, double* energy, double* volume) {
+  if (!s || !u || !energy || !volume) return fail(CI_ERR_INVALID, "null argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  const int N = s->N;
+  const ci::Plan& P = s->plan;
+  std::vector<double> hv(3 * (size_t)N);
+  for (int i = 0; i < N; i++)
+    for (int k = 0; k < 3; k++) hv[(size_t)k * N + i] = u[3 * (size_t)P.node_orig[i] + k];
+  CI_CUDA(s->d_u2.alloc(3 * (size_t)N));
+  CI_CUDA(s->d_v2.alloc(3 * (size_t)N));
+  CI_CUDA(cudaMemsetAsync(s->d_u2.p, 0, sizeof(double) * 3 * N, s->stream));
+  CI_CUDA(cudaMemcpyAsync(s->d_v2.p, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  DBuf<double> work;
+  CI_CUDA(work.alloc(4 * (size_t)s->C));
+  CI_CUDA(cudaMemsetAsync(work.p, 0, sizeof(double) * 4 * s->C, s->stream));
+  ci::DevState D = s->dev_state(s->d_u2.p, s->d_v2.p);
+  D.chunk_work = work.p;
+  CI_CUDA(launch_elem_mode(s, ci::EM_REFCOMPAT, D, s->elem_params(1.0f, true)));
+  std::vector<double> hw(4 * (size_t)s->C);
+  CI_CUDA(cudaMemcpyAsync(hw.data(), work.p, sizeof(double) * hw.size(), cudaMemcpyDeviceToHost,
+                          s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  double W = 0, V = 0;
+  for (int c = 0; c < s->C; c++) {
+    W += hw[4 * c];
+    V += hw[4 * c + 2];
+  }
+  *energy = W;
+  *volume = V;
+  return check_status(s);
+}
+
+int ci_time_steps(ci_solver* s, int nsteps, float* ms) {
+  int rc = require_started(s);
+  if (rc) return rc;
+  if (!ms) return fail(CI_ERR_INVALID, "null argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  CI_CUDA(cudaEventRecord(s->ev0, s->stream));
+  if ((rc = enqueue_steps(s, nsteps))) return rc;
+  CI_CUDA(cudaEventRecord(s->ev1, s->stream));
+  CI_CUDA(cudaEventSynchronize(s->ev1));
+  CI_CUDA(cudaEventElapsedTime(ms, s->ev0, s->ev1));
+  return check_status(s);
+}
+
+int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms) {
+  int rc = require_started(s);
+  if (rc) return rc;
+  if (!out_ms || nsteps <= 0) return fail(CI_ERR_INVALID, "bad argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  std::vector<cudaEvent_t> ev(3 * nsteps);
+  for (auto& e : ev) CI_CUDA(cudaEventCreate(&e));
+  const ci::DevState D = s->dev_state(s->d_u.p, s->d_v.p);
+  const int nb = (s->N + 255) / 256;
+  for (int i = 0; i < nsteps; i++) {
+    CI_CUDA(cudaEventRecord(ev[3 * i], s->stream));
+    CI_CUDA(launch_elem_mode(s, step_mode(s), D, s->elem_params((float)s->dt, true)));
+    CI_CUDA(cudaEventRecord(ev[3 * i + 1], s->stream));
+    ci::k_node<false, true><<<nb, 256, 0, s->stream>>>(s->node_arrays(), s->node_params());
+    CI_CUDA(cudaGetLastError());
+    CI_CUDA(cudaEventRecord(ev[3 * i + 2], s->stream));
+  }
+  CI_CUDA(cudaEventSynchronize(ev.back()));
+  double te = 0, tn = 0;
+  for (int i = 0; i < nsteps; i++) {
+    float a, b;
+    CI_CUDA(cudaEventElapsedTime(&a, ev[3 * i], ev[3 * i + 1]));
+    CI_CUDA(cudaEventElapsedTime(&b, ev[3 * i + 1], ev[3 * i + 2]));
+    te += a;
+    tn += b;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  s->steps_done += nsteps;
+  out_ms[0] = (float)(te / nsteps);
+  out_ms[1] = (float)(tn / nsteps);
+  return check_status(s);
+}
+
+int ci_launches_per_step(const ci_solver* s) { return s ? 2 : 0; }
+
+int ci_plan_stats(const ci_mesh* mesh, int chunk_elements, int chunk_nodes, long long* stats,
+                  int* perm_elems, int* perm_nodes) {
+  if (!mesh || !stats) return fail(CI_ERR_INVALID, "null argument");
+  ci::Plan P;
+  std::string err;
+  if (!ci::build_plan(mesh->num_nodes, mesh->num_elements, mesh->nodes_per_element, mesh->xloc,
+                      mesh->element_nodes, chunk_elements, chunk_nodes, 304, &P, &err))
+    return fail(CI_ERR_INVALID, "%s", err.c_str());
+  stats[0] = P.n_chunks;
+  stats[1] = P.max_colors;
+  stats[2] = P.max_local;
+  stats[3] = P.slot_row[P.N];
+  stats[4] = P.max_chunk_elems;
+  stats[5] = P.n_ghosts;
+  stats[6] = P.n_boundary;
+  stats[7] = 0;
+  if (perm_elems) std::memcpy(perm_elems, P.elem_orig.data(), sizeof(int) * P.E);
+  if (perm_nodes) std::memcpy(perm_nodes, P.node_orig.data(), sizeof(int) * P.N);
+  return CI_OK;
+}
+
+int ci_plan_verify(const ci_mesh* mesh, int chunk_elements, int chunk_nodes) {
+  if (!mesh) return fail(CI_ERR_INVALID, "null argument");
+  ci::Plan P;
+  std::string err;
+  if (!ci::build_plan(mesh->num_nodes, mesh->num_elements, mesh->nodes_per_element, mesh->xloc,
+                      mesh->element_nodes, chunk_elements, chunk_nodes, 304, &P, &err))
+    return fail(CI_ERR_INVALID, "%s", err.c_str());
+  if (!ci::verify_plan(P, mesh->element_nodes, &err)) return fail(CI_ERR_INVALID, "%s", err.c_str());
+  return CI_OK;
+}
+
+}  // extern "C"

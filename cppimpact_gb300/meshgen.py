@@ -197,6 +197,26 @@ def cfl_dt(mesh: TetMesh, E: float, nu: float, rho: float, fraction: float = 0.5
     return fraction * h / dilatational_speed(E, nu, rho)
 
 
+def wall_stiffness(mesh: TetMesh, E: float) -> float:
+    """Penalty stiffness ``E x (min element height)`` (N/m).
+
+    The reference drivers use ``10 E`` (test.cu:91), which on these meshes at
+    ``dt = 0.5 CFL`` puts the wall's penalty frequency above the explicit stability
+    limit (omega dt > 2), so trajectories through contact amplify round-off.  Scaling
+    the penalty with the element stiffness keeps omega dt below 1.
+    """
+    return float(E * min_element_height(mesh))
+
+
+def impact_setup(mesh: TetMesh, speed: float, gap: float, E: float = AL_J2["E"],
+                 nu: float = AL_J2["nu"], rho: float = AL_J2["rho"]) -> dict:
+    """Impact along -z onto the plane z = min z - gap (normal +z), dt = 0.5 CFL."""
+    zmin = float(mesh.xloc[:, 2].min())
+    return dict(vel=(0.0, 0.0, -float(speed)), wall_normal=(0.0, 0.0, 1.0),
+                wall_offset=zmin - gap, wall_stiffness=wall_stiffness(mesh, E),
+                dt=cfl_dt(mesh, E, nu, rho))
+
+
 # ---------------------------------------------------------------------------
 # .inp I/O
 # ---------------------------------------------------------------------------

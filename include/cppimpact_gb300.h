@@ -1,0 +1,192 @@
+/*
+ * cppimpact_gb300.h -- C ABI of the GB300-native explicit impact step.
+ *
+ * One shared library, libcppimpact_gb300.so, exports everything below with C linkage:
+ * plain pointers and sizes, no C++ or framework types.  Status codes are int:
+ * CI_OK (0) or a negative CI_ERR_*; ci_last_error() returns the message of the last
+ * failure on the calling thread.  Host buffers are owned by the caller; device memory
+ * is owned by the library and freed by ci_destroy.  One solver is used from one host
+ * thread at a time; distinct solvers are independent.
+ *
+ * The entry points replace the reference's C++ template interface for the hot path
+ * (smdogroup/cppimpact, paths relative to the reference checkout):
+ *   Dynamics<T,Basis,Analysis,Quadrature>(Mesh*, BaseMaterial*, Wall*)   include/dynamics.h:64-83
+ *   Dynamics::initialize(pos, vel)                                       include/dynamics.h:99-111
+ *   Dynamics::solve(dt, time_end, export_interval)                       include/dynamics.h:414-512
+ *   update<T,3,npe,Basis,Analysis>(...)  (one step's accelerations)      include/dynamics_kernels.h:8-169
+ *   FEAnalysis::element_mass_matrix / calculate_f_internal              include/analysis.h:136-162, 321-382
+ *   Dynamics::debug_strain (strain energy + volume)                      include/dynamics.h:303-412
+ *   Mesh::load_mesh(filename)                                            include/mesh.h:57-267
+ * The C++ drop-in headers in include/cppimpact/ keep those class names and
+ * signatures and forward to these functions.
+ */
+#ifndef CPPIMPACT_GB300_H
+#define CPPIMPACT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CI_ABI_VERSION 1
+
+/* status codes */
+#define CI_OK 0
+#define CI_ERR_INVALID -1     /* bad argument or inconsistent mesh */
+#define CI_ERR_CUDA -2        /* a CUDA runtime call failed */
+#define CI_ERR_DEGENERATE -3  /* an element has det J <= 0 */
+#define CI_ERR_NONFINITE -4   /* NaN/Inf appeared in the nodal state */
+#define CI_ERR_UNSUPPORTED -5 /* valid request this build does not implement */
+#define CI_ERR_IO -6          /* file could not be opened or parsed */
+#define CI_ERR_NOMEM -7       /* host or device allocation failed */
+#define CI_ERR_TOO_LARGE -8   /* a size limit of the entry point was exceeded */
+
+/* constitutive mode */
+#define CI_MODE_J2 0        /* J2 radial return, linear isotropic hardening, stored stress */
+#define CI_MODE_REFCOMPAT 1 /* the reference's incremental force K_e(x_n) * (dt v) */
+
+/* mass lumping */
+#define CI_LUMP_ROWSUM 0 /* m_i = rho sum_q N_i w_q detJ_q (the reference's rule) */
+#define CI_LUMP_HRZ 1    /* Hinton-Rock-Zienkiewicz diagonal scaling (positive for tet10) */
+
+/* Mesh: exactly the fields of Mesh<T,npe> (include/mesh.h:14-18).  Node and element
+ * ids are 0-based as after Mesh::load_mesh.  slave/fixed sets are carried for
+ * completeness; like the reference wall, contact is tested on every node. */
+typedef struct ci_mesh {
+  int num_nodes;
+  int num_elements;
+  int nodes_per_element;    /* 4 (C3D4) or 10 (C3D10, CalculiX edge order) */
+  const double* xloc;       /* [3*num_nodes]  x0 y0 z0 x1 ... */
+  const int* element_nodes; /* [npe*num_elements] */
+  int num_slave_nodes;
+  const int* slave_nodes;
+  int num_fixed_nodes;
+  const int* fixed_nodes;
+} ci_mesh;
+
+/* Material: BaseMaterial{E, rho, nu} (include/basematerial.h:6-20) plus the J2
+ * parameters Elastoplastic stores (include/elastoplastic.h:7-23).  beta is the
+ * kinematic-hardening fraction; only beta = 0 (isotropic) is implemented. */
+typedef struct ci_material {
+  double E, nu, rho;
+  double sigma_y0; /* initial yield stress (Pa); <= 0 or huge means elastic */
+  double H;        /* isotropic hardening modulus (Pa): sigma_y = sigma_y0 + H epbar */
+  double beta;
+} ci_material;
+
+/* Rigid planar wall: contact when d = normal . (x + du) - offset < 0; the node then
+ * gets a += -(d k / m) normal.  The reference's Wall<T,dim,Basis>(name, location,
+ * stiffness, slave, n, normal) (include/wall.h:23-43) is normal = normal_sign e_dim,
+ * offset = normal_sign * location. */
+typedef struct ci_wall {
+  double normal[3];
+  double offset;
+  double stiffness; /* N/m */
+} ci_wall;
+
+typedef struct ci_options {
+  int mode;           /* CI_MODE_* */
+  int lumping;        /* CI_LUMP_* */
+  double gravity[3];  /* body acceleration; the reference uses (0, 0, -9.81) */
+  int device;         /* CUDA device ordinal */
+  int chunk_elements; /* elements per CTA chunk, 0 = automatic */
+  int chunk_nodes;    /* local-node budget per chunk, 0 = automatic */
+  int graph_steps;    /* steps captured per CUDA graph, 0 = automatic */
+} ci_options;
+
+/* energy terms (FP64), see ci_get_energy */
+typedef struct ci_energy {
+  double kinetic;  /* 1/2 sum m |v_n|^2 at the last completed step */
+  double internal; /* sum over steps and QPs of w detJ 1/2 (sigma_n + sigma_{n+1}) : d_eps */
+  double plastic;  /* sum over steps and QPs of w detJ sigma_y d_epbar */
+  double contact;  /* work done by the wall on the body */
+  double gravity;  /* work done by gravity on the body */
+  double kinetic0; /* initial kinetic energy */
+  double balance;  /* kinetic + internal - contact - gravity - kinetic0 */
+} ci_energy;
+
+typedef struct ci_solver ci_solver;
+
+/* ---- library ---- */
+int ci_abi_version(void);
+const char* ci_last_error(void);
+void ci_default_options(ci_options* o);
+
+/* ---- solver lifetime: Dynamics(Mesh*, BaseMaterial*, Wall*), include/dynamics.h:64-83 ---- */
+int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
+              const ci_options* opt, ci_solver** out);
+int ci_destroy(ci_solver* s);
+
+/* Dynamics::initialize (include/dynamics.h:99-111): positions X + pos, velocity vel,
+ * stored stress and plastic strain zero, contact history cleared. */
+int ci_initialize(ci_solver* s, const double pos[3], const double vel[3]);
+
+/* Dynamics::solve (include/dynamics.h:414-512): lumped mass, a0 from zero increment,
+ * v += dt/2 a0, then steps while time <= time_end (time += dt in double, the
+ * reference's loop count).  export_interval is accepted for signature parity; state
+ * is read back with ci_get_state. */
+int ci_solve(ci_solver* s, double dt, double time_end, int export_interval);
+
+/* Lower-level stepping: ci_start does the mass, a0 and half step of Dynamics::solve;
+ * ci_step advances nsteps more steps of size dt (graph-captured). */
+int ci_start(ci_solver* s, double dt);
+int ci_step(ci_solver* s, int nsteps);
+int ci_steps_done(const ci_solver* s, long long* nsteps);
+
+/* Read back (any pointer may be NULL): x, v [3N] in the caller's node order (current
+ * positions and the half-step velocity held by the reference's vel array), mass [N],
+ * sigma [E*nq*6] (Voigt xx yy zz xy yz xz), epbar [E*nq] in the caller's element
+ * order (nq = 1 for tet4, 4 for tet10), contact [N]: bit0 in contact at the last
+ * step, bit1 ever in contact. */
+int ci_get_state(ci_solver* s, double* x, double* v, double* mass, float* sigma, float* epbar,
+                 unsigned char* contact);
+/* Overwrite the nodal state (caller order, [3N] each); used for restarts. */
+int ci_set_state(ci_solver* s, const double* x, const double* v);
+int ci_get_energy(ci_solver* s, ci_energy* e);
+/* Device status word: bit0 non-positive det J seen, bit1 non-finite state seen. */
+int ci_get_status(ci_solver* s, unsigned int* status);
+
+/* ---- one-shot kernels (the per-step seam, include/dynamics_kernels.h:8-169) ---- */
+/* Assembled internal force f[3N] of FEAnalysis::calculate_f_internal for positions
+ * x[3N] and increment du[3N] on the solver's mesh and mode; sigma_in/epbar_in
+ * (caller element order, may be NULL = zero) are the stored QP states, sigma_out /
+ * epbar_out (may be NULL) receive the updated ones. */
+int ci_internal_force(ci_solver* s, const double* x, const double* du, const float* sigma_in,
+                      const float* epbar_in, double* f, float* sigma_out, float* epbar_out);
+/* Lumped nodal mass [N] at positions x[3N] (FEAnalysis::element_mass_matrix assembled). */
+int ci_lumped_mass(ci_solver* s, const double* x, double* mass);
+/* Dynamics::debug_strain: total strain energy 1/2 u . K u and volume at the mesh
+ * positions for a prescribed displacement u[3N] (RefCompat force). */
+int ci_strain_energy(ci_solver* s, const double* u, double* energy, double* volume);
+
+/* ---- timing helpers for benchmarks (CUDA events on the solver's stream) ---- */
+int ci_time_steps(ci_solver* s, int nsteps, float* ms);
+/* Mean device duration (ms) of each kernel kind over the last ci_time_kernels call:
+ * out[0] element kernel, out[1] node kernel. */
+int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms);
+/* Kernel launches one step issues (for launch accounting). */
+int ci_launches_per_step(const ci_solver* s);
+
+/* ---- mesh utilities (host only) ---- */
+/* Mesh::load_mesh (include/mesh.h:57-267): parse an Abaqus/CalculiX .inp file.
+ * Arrays are malloc'ed by the library and released with ci_mesh_free. */
+int ci_mesh_load_inp(const char* path, int nodes_per_element, ci_mesh* out);
+void ci_mesh_free(ci_mesh* m);
+
+/* Preprocessing summary (host only, no GPU needed): space-filling-curve order,
+ * chunking, node ownership and per-chunk colouring.  stats[0..7] = chunks,
+ * max colours, max local nodes, total slots, max chunk elements, ghosts, boundary
+ * nodes, 0. perm_elems (may be NULL, [E]) receives the plan order of elements
+ * (original ids), perm_nodes (may be NULL, [N]) the plan order of nodes. */
+int ci_plan_stats(const ci_mesh* mesh, int chunk_elements, int chunk_nodes, long long* stats,
+                  int* perm_elems, int* perm_nodes);
+/* Check a plan's invariants on the host: every element once, colours conflict-free
+ * within each chunk, slot lists cover every (chunk, node) pair.  Returns CI_OK. */
+int ci_plan_verify(const ci_mesh* mesh, int chunk_elements, int chunk_nodes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CPPIMPACT_GB300_H */

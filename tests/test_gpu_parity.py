@@ -1,0 +1,227 @@
+"""GPU parity: the sm_103a kernels through the C ABI against the FP64 oracle and the
+reference fixtures.  Tolerances (FP32 element math, FP64 nodal state):
+  * one-shot f_int, masses, strain energies: relative L2 <= 1e-5
+  * trajectories: end-state displacement and equivalent plastic strain within 1e-3
+    relative L2 of the FP64 run; identical contact-node sets (ever touched)."""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from cppimpact_gb300 import meshgen as mg
+
+pytestmark = pytest.mark.gpu
+
+E, NU, RHO = 68.9e9, 0.33, 2700.0
+SY0, H = 276e6, 0.689e9
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+def solver(cilib, m, mode, lumping=None, **kw):
+    if lumping is None:
+        lumping = cilib.LUMP_ROWSUM if mode == cilib.MODE_REFCOMPAT else cilib.LUMP_HRZ
+    return cilib.Solver(m.xloc, m.conn, E=E, nu=NU, rho=RHO, sigma_y0=SY0, H=H, mode=mode,
+                        lumping=lumping, **kw)
+
+
+@pytest.mark.parametrize("order,n", [(1, 4), (2, 3)])
+@pytest.mark.parametrize("lump", ["rowsum", "hrz"])
+def test_lumped_mass(cilib, oracle, order, n, lump):
+    m = mg.cube(n, order)
+    lp = cilib.LUMP_HRZ if lump == "hrz" else cilib.LUMP_ROWSUM
+    s = solver(cilib, m, cilib.MODE_J2, lumping=lp)
+    got = s.lumped_mass()
+    ref = oracle.lumped_mass(m.xloc, m.conn, oracle.params(E, NU, RHO, lumping=lp))
+    assert rel(got, ref) < 1e-6
+
+
+def test_mass_matches_reference_fixture(cilib):
+    g = golden("ref_update_tet10_c2.npz")
+    s = cilib.Solver(g["xloc"], g["conn"], E=E, nu=NU, rho=RHO, mode=cilib.MODE_REFCOMPAT,
+                     lumping=cilib.LUMP_ROWSUM)
+    got = s.lumped_mass()
+    assert rel(got, g["mass"]) < 1e-6
+    assert got.min() < 0  # the reference's row-sum corner masses of tet10
+
+
+@pytest.mark.parametrize("order,n", [(1, 4), (2, 3)])
+def test_internal_force_refcompat(cilib, oracle, order, n):
+    m = mg.cube(n, order)
+    rng = np.random.default_rng(11)
+    x = m.xloc + rng.normal(scale=1e-4, size=m.xloc.shape)
+    du = rng.normal(scale=1e-6, size=m.xloc.shape)
+    s = solver(cilib, m, cilib.MODE_REFCOMPAT)
+    f, _, _ = s.internal_force(x, du)
+    fr, _, _, _ = oracle.internal_force(m.xloc, m.conn, oracle.params(E, NU, RHO, mode=oracle.REFCOMPAT),
+                                        x, du)
+    assert rel(f, fr.reshape(-1, 3)) < 1e-5
+
+
+def test_internal_force_matches_reference_update(cilib):
+    """Kernel-level parity with the reference's update() on tet10 (f_int from acc)."""
+    g = golden("ref_update_tet10_c2.npz")
+    p = json.loads(str(g["params"]))
+    s = cilib.Solver(g["xloc"], g["conn"], E=E, nu=NU, rho=RHO, mode=cilib.MODE_REFCOMPAT,
+                     lumping=cilib.LUMP_ROWSUM)
+    f, _, _ = s.internal_force(g["xloc"], g["dof"])
+    x_end = g["xloc"] + g["dof"]
+    acc = g["acc"].copy()
+    acc[:, 2] += 9.81
+    d = x_end[:, 2] - p["wall_location"]
+    hit = d < 0
+    acc[hit, 2] -= -(1.0 / g["mass"][hit]) * d[hit] * p["wall_stiffness"]
+    f_ref = -acc * g["mass"][:, None]
+    assert rel(f, f_ref) < 1e-5
+
+
+@pytest.mark.parametrize("order,n", [(1, 4), (2, 3)])
+def test_internal_force_j2_with_stored_stress(cilib, oracle, order, n):
+    m = mg.cube(n, order)
+    nq = 1 if order == 1 else 4
+    rng = np.random.default_rng(5)
+    du = rng.normal(scale=4e-5, size=m.xloc.shape)
+    sig = rng.normal(scale=1.2e8, size=(m.num_elements, nq, 6)).astype(np.float32)
+    ep = rng.uniform(0, 0.01, size=(m.num_elements, nq)).astype(np.float32)
+    s = solver(cilib, m, cilib.MODE_J2)
+    f, so, eo = s.internal_force(m.xloc, du, sig, ep)
+    fr, sr, er, _ = oracle.internal_force(m.xloc, m.conn, oracle.params(E, NU, RHO, SY0, H, mode=oracle.J2),
+                                          m.xloc, du, sig.astype(np.float64), ep.astype(np.float64))
+    assert rel(f, fr.reshape(-1, 3)) < 1e-5
+    assert rel(so, sr) < 1e-5
+    assert rel(eo, er) < 1e-5
+    assert (er > ep).any()  # some points yielded
+
+
+def test_strain_energy_known_answers(cilib):
+    g = golden("ref_strain_kat.npz")
+    rows = json.loads(str(g["rows"]))
+    from golden.make_golden import single_tet
+    meshes = {"single_tet1": single_tet(1), "single_tet2": single_tet(2),
+              "cube4_tet4": mg.cube(4, 1), "cube4_tet10": mg.cube(4, 2)}
+    for name, npe, case, W_ref, V_ref in rows:
+        m = meshes[name]
+        x = m.xloc
+        gx = x[:, 0] if case == 0 else 0.5 * x[:, 0] ** 2
+        u = np.stack([0.01 * gx, -0.01 * NU * gx, -0.01 * NU * gx], axis=1)
+        s = cilib.Solver(m.xloc, m.conn, E=E, nu=NU, rho=RHO, mode=cilib.MODE_REFCOMPAT)
+        W, V = s.strain_energy(u)
+        assert W == pytest.approx(W_ref, rel=1e-5), (name, case)
+        assert V == pytest.approx(V_ref, rel=1e-5), (name, case)
+
+
+def _run_gpu(cilib, m, setup, mode, nsteps, lumping=None, **kw):
+    s = solver(cilib, m, mode, lumping=lumping, wall_normal=setup["wall_normal"],
+               wall_offset=setup["wall_offset"], wall_stiffness=setup["wall_stiffness"], **kw)
+    s.initialize(setup["vel"])
+    s.start(setup["dt"])
+    s.step(nsteps)
+    return s
+
+
+def _run_oracle(oracle, m, setup, mode, nsteps, lumping):
+    par = oracle.params(E, NU, RHO, SY0, H, mode=mode, lumping=lumping,
+                        wall_normal=setup["wall_normal"], wall_offset=setup["wall_offset"],
+                        wall_stiffness=setup["wall_stiffness"])
+    o = oracle.Solver(m.xloc, m.conn, par)
+    o.initialize(setup["vel"], setup["dt"])
+    o.step(nsteps)
+    return o.get()
+
+
+def test_refcompat_trajectory_vs_reference_small(cilib):
+    """The small workload (6000 tet4, 2000 steps through contact) against the compiled
+    reference's own trajectory."""
+    g = golden("ref_small_tet4.npz")
+    p = json.loads(str(g["params"]))
+    m = mg.TetMesh(g["xloc"], g["conn"], np.zeros(0, np.int32))
+    setup = dict(vel=p["vel"], dt=p["dt"], wall_normal=(0, 0, 1), wall_offset=p["wall_location"],
+                 wall_stiffness=p["wall_stiffness"])
+    s = _run_gpu(cilib, m, setup, cilib.MODE_REFCOMPAT, p["nsteps"])
+    st = s.state()
+    u_ref = g["x"] - g["xloc"]
+    assert rel(st["x"] - g["xloc"], u_ref) < 1e-3
+    assert rel(st["v"], g["v"]) < 1e-3
+
+
+def test_refcompat_trajectory_vs_reference_tet4(cilib):
+    g = golden("ref_traj_tet4_c4.npz")
+    p = json.loads(str(g["params"]))
+    m = mg.TetMesh(g["xloc"], g["conn"], np.zeros(0, np.int32))
+    setup = dict(vel=p["vel"], dt=p["dt"], wall_normal=(0, 0, 1), wall_offset=p["wall_location"],
+                 wall_stiffness=p["wall_stiffness"])
+    s = _run_gpu(cilib, m, setup, cilib.MODE_REFCOMPAT, p["nsteps"])
+    st = s.state()
+    assert rel(st["x"] - g["xloc"], g["x"] - g["xloc"]) < 1e-3
+
+
+@pytest.mark.parametrize("order,n,steps,speed", [(1, 6, 800, 10.0), (2, 3, 600, 20.0)])
+def test_j2_trajectory_vs_fp64(cilib, oracle, order, n, steps, speed):
+    m = mg.cube(n, order)
+    setup = mg.impact_setup(m, speed, 1e-4)
+    s = _run_gpu(cilib, m, setup, cilib.MODE_J2, steps)
+    st = s.state()
+    ref = _run_oracle(oracle, m, setup, oracle.J2, steps, oracle.LUMP_HRZ)
+    assert ref["epbar"].max() > 0, "the case must yield"
+    assert rel(st["x"] - m.xloc, ref["x"] - m.xloc) < 1e-3
+    assert rel(st["epbar"], ref["epbar"]) < 1e-3
+    ever = (st["contact"] & 2) > 0
+    ever_ref = (ref["contact"] & 2) > 0
+    assert ever_ref.sum() > 0
+    assert np.array_equal(ever, ever_ref)
+    en = s.energy()
+    assert en["kinetic"] == pytest.approx(ref["energy"][oracle.E_KINETIC], rel=1e-3)
+    assert en["internal"] == pytest.approx(ref["energy"][oracle.E_INTERNAL], rel=1e-3)
+    assert abs(en["balance"]) < 0.02 * en["kinetic0"]
+
+
+def test_deterministic_bitwise(cilib):
+    m = mg.cube(6, 2)
+    setup = mg.impact_setup(m, 20.0, 1e-4)
+    a = _run_gpu(cilib, m, setup, cilib.MODE_J2, 300).state()
+    b = _run_gpu(cilib, m, setup, cilib.MODE_J2, 300).state()
+    for k in ("x", "v", "sigma", "epbar", "contact"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_chunking_does_not_change_physics(cilib):
+    """Different chunk sizes change the summation grouping only (FP32 round-off)."""
+    m = mg.cube(5, 2)
+    setup = mg.impact_setup(m, 20.0, 1e-4)
+    a = _run_gpu(cilib, m, setup, cilib.MODE_J2, 200).state()
+    b = _run_gpu(cilib, m, setup, cilib.MODE_J2, 200, chunk_elements=37, chunk_nodes=200).state()
+    assert rel(a["x"] - m.xloc, b["x"] - m.xloc) < 1e-5
+
+
+def test_solve_loop_count_matches_reference(cilib):
+    g = golden("ref_traj_tet4_c4.npz")
+    p = json.loads(str(g["params"]))
+    s = cilib.Solver(g["xloc"], g["conn"], E=E, nu=NU, rho=RHO, mode=cilib.MODE_REFCOMPAT,
+                     lumping=cilib.LUMP_ROWSUM, wall_normal=(0, 0, 1),
+                     wall_offset=p["wall_location"], wall_stiffness=p["wall_stiffness"])
+    s.initialize(p["vel"])
+    s.solve(p["dt"], p["t_end"])
+    assert s.steps_done() == p["nsteps"]
+    assert rel(s.state()["x"] - g["xloc"], g["x"] - g["xloc"]) < 1e-3
+
+
+def test_degenerate_element_reported(cilib):
+    m = mg.cube(2, 1)
+    conn = m.conn.copy()
+    conn[0, [1, 2]] = conn[0, [2, 1]]  # inverted element: det J < 0
+    s = cilib.Solver(m.xloc, conn, E=E, nu=NU, rho=RHO)
+    with pytest.raises(cilib.CiError) as ei:
+        s.lumped_mass()
+    assert ei.value.code == -3
+
+
+def test_nonfinite_state_reported(cilib):
+    m = mg.cube(2, 1)
+    s = cilib.Solver(m.xloc, m.conn, E=E, nu=NU, rho=RHO)
+    s.initialize((0.0, 0.0, float("nan")))
+    with pytest.raises(cilib.CiError) as ei:
+        s.start(1e-7)
+    assert ei.value.code == -4
