@@ -49,6 +49,10 @@ def workload(name: str):
         m = mg.shell()
         setup = mg.impact_setup(m, 5.0, 0.0)
         desc = "shell R1 L4 t0.004 720x140x1 tet10 J2 5 m/s"
+    elif name == "shell_half":
+        m = mg.shell(n_theta=360)
+        setup = mg.impact_setup(m, 5.0, 0.0)
+        desc = "shell R1 L4 t0.004 360x140x1 tet10 J2 5 m/s (profiling size)"
     elif name == "quad":
         m = mg.cube(18, 2)
         setup = mg.impact_setup(m, 20.0, 1e-3)
@@ -191,6 +195,8 @@ def run_ours(args, rank, world):
     m, setup, desc = workload(args.workload)
     N, E, npe = m.num_nodes, m.num_elements, m.npe
     s = api.Solver(m.xloc, m.conn, **MAT, mode=api.MODE_J2, lumping=api.LUMP_HRZ,
+                   step_kernel=args.step_kernel, chunk_elements=args.chunk_elements,
+                   chunk_nodes=args.chunk_nodes, block_threads=args.block_threads,
                    wall_normal=setup["wall_normal"], wall_offset=setup["wall_offset"],
                    wall_stiffness=setup["wall_stiffness"],
                    device=int(os.environ.get("LOCAL_RANK", "0")))
@@ -215,13 +221,17 @@ def run_ours(args, rank, world):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    achieved = elem_bytes / (k_elem_ms * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "k_elem (element force + J2 + colour assembly)",
+    fused = args.step_kernel == 0
+    kbytes = step_bytes if fused else elem_bytes
+    achieved = kbytes / (k_elem_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm",
+                "kernel": ("k_step (fused element force + J2 + assembly + node update)" if fused
+                           else "k_elem (element force + J2 + colour assembly)"),
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_src,
                 "traffic": args.traffic, "kernel_ms": round(k_elem_ms, 4),
-                "node_kernel_ms": round(k_node_ms, 4),
-                "bytes_formula": "E(4 npe + 56 nq) + 60 N"}
+                "other_kernel_ms_per_step": round(k_node_ms, 4),
+                "bytes_formula": "E(4 npe + 56 nq) + 112 N" if fused else "E(4 npe + 56 nq) + 60 N"}
     step_roof = {"achieved": round(step_bytes / (ms_step * 1e-3) / 1e9, 1),
                  "frac": round(step_bytes / (ms_step * 1e-3) / 1e9 / peak, 4),
                  "bytes_per_elem_step": round(step_bytes / E, 1)}
@@ -311,9 +321,13 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--warmup", type=int, default=20)
-    ap.add_argument("--workload", default="shell", choices=["shell", "quad", "small"])
+    ap.add_argument("--workload", default="shell", choices=["shell", "shell_half", "quad", "small"])
+    ap.add_argument("--step-kernel", type=int, default=0, help="0 fused, 1 element + node kernels")
+    ap.add_argument("--chunk-elements", type=int, default=0)
+    ap.add_argument("--chunk-nodes", type=int, default=0)
+    ap.add_argument("--block-threads", type=int, default=0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-interval", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

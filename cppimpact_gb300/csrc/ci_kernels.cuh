@@ -444,6 +444,244 @@ __global__ void __launch_bounds__(256) k_node(NodeArrays A, NodeParams p) {
   if (!finite) atomicOr(A.status, (unsigned)ST_NONFINITE);
 }
 
+// ---------------------------------------------------------------------------
+// Fused step (one launch per time step, no grid-wide barrier).
+//
+// Node state S^n = (u^n, v^{n+1/2}) is double-buffered.  A chunk's INTERIOR nodes are
+// touched by no other chunk: the chunk updates them in its epilogue, S^n -> S^{n+1}
+// written to the other buffer.  BOUNDARY nodes are touched by several chunks: each
+// chunk writes its partial force to the node's slot in the halo buffer of step n,
+// and at the start of step n+1 every chunk touching the node sums the slots (fixed
+// chunk order) and applies the same update to S^n itself; the owner stores the
+// result.  The update uses explicitly rounded operations so every chunk obtains the
+// same bits.  After the last step of a call k_finalize_boundary completes S^N for the
+// boundary nodes.
+// ---------------------------------------------------------------------------
+struct FusedArgs {
+  DevPlan P;
+  double* u_cur[3];
+  double* v_cur[3];
+  double* u_prv[3];
+  double* v_prv[3];
+  const float* halo_prv[3];
+  float* halo_cur[3];
+  const float* mass;
+  const double* d0;
+  unsigned char* contact;
+  float* acc[3];
+  float4* sig_a;
+  float2* sig_b;
+  float* epbar;
+  double* chunk_work;
+  unsigned int* status;
+  int bnd_final;  // boundary nodes already hold S^n in the cur buffer
+  int store_acc;
+};
+
+// One node's central-difference update from its total internal force f.
+// u, v: in S^n, out S^{n+1}.  Rounding is explicit (no contraction freedom).
+__device__ __forceinline__ void node_step(const NodeParams& p, float fx, float fy, float fz, float m,
+                                          double d0, double (&u)[3], double (&v)[3],
+                                          double (&a)[3], bool& in_contact) {
+  const float rm = __frcp_rn(m);
+  a[0] = __dadd_rn((double)__fmul_rn(-fx, rm), p.g[0]);
+  a[1] = __dadd_rn((double)__fmul_rn(-fy, rm), p.g[1]);
+  a[2] = __dadd_rn((double)__fmul_rn(-fz, rm), p.g[2]);
+  double un[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) un[k] = __fma_rn(p.dt, v[k], u[k]);
+  const double d = __fma_rn(p.wall_n[2], un[2], __fma_rn(p.wall_n[1], un[1],
+                            __fma_rn(p.wall_n[0], un[0], d0)));
+  in_contact = d < 0.0;
+  if (in_contact) {
+    const double c = __ddiv_rn(__dmul_rn(-d, p.wall_k), (double)m);
+#pragma unroll
+    for (int k = 0; k < 3; k++) a[k] = __fma_rn(c, p.wall_n[k], a[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    v[k] = __fma_rn(p.dt, a[k], v[k]);
+    u[k] = un[k];
+  }
+}
+
+__device__ __forceinline__ void store_node(const FusedArgs& A, double* const (&uo)[3],
+                                           double* const (&vo)[3], int g, const double (&u)[3],
+                                           const double (&v)[3], const double (&a)[3],
+                                           bool in_contact, bool store_acc) {
+  bool finite = true;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    uo[k][g] = u[k];
+    vo[k][g] = v[k];
+    finite = finite && isfinite(v[k]);
+    if (store_acc) A.acc[k][g] = (float)a[k];
+  }
+  if (!finite) atomicOr(A.status, (unsigned)ST_NONFINITE);
+  const unsigned char old = A.contact[g];
+  const unsigned char flag = in_contact ? 3 : (old & 2);
+  if (flag != old) A.contact[g] = flag;
+}
+
+template <int NPE, int MODE, int BS>
+__global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep, NodeParams np) {
+  extern __shared__ float sm[];
+  const DevPlan& P = A.P;
+  const ChunkInfo ch = P.chunks[blockIdx.x];
+  const int L = ch.n_local;
+  float* sx = sm;
+  float* sd = sm + 3 * L;
+  float* sa = sm + 6 * L;
+  __shared__ float red[BS / 32];
+
+  // -- stage S^n of every local node (finalising boundary nodes) ----------------------
+  // interior nodes: contiguous owned range, independent loads (unrolled for MLP)
+  const int n_direct = A.bnd_final ? L : ch.n_int;
+#pragma unroll 4
+  for (int l = threadIdx.x; l < n_direct; l += BS) {
+    const int lb = ch.local_begin + l;
+    const int g = l < ch.n_int ? ch.own_begin + l : P.local_gid[lb];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double u = A.u_cur[k][g];
+      const double v = A.v_cur[k][g];
+      sx[k * L + l] = P.local_x0[(size_t)k * P.Lt + lb] + (float)u;
+      sd[k * L + l] = ep.dt * (float)v;
+      sa[k * L + l] = 0.f;
+    }
+  }
+  // boundary nodes: sum the previous step's partial forces and apply the update
+#pragma unroll 2
+  for (int l = n_direct + threadIdx.x; l < L; l += BS) {
+    const int lb = ch.local_begin + l;
+    const int g = P.local_gid[lb];
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    const int s1 = P.slot_row[g + 1];
+    for (int s = P.slot_row[g]; s < s1; s++) {
+      fx = __fadd_rn(fx, A.halo_prv[0][s]);
+      fy = __fadd_rn(fy, A.halo_prv[1][s]);
+      fz = __fadd_rn(fz, A.halo_prv[2][s]);
+    }
+    double u[3], v[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      u[k] = A.u_prv[k][g];
+      v[k] = A.v_prv[k][g];
+    }
+    double a[3];
+    bool hit;
+    node_step(np, fx, fy, fz, A.mass[g], A.d0[g], u, v, a, hit);
+    if (l < ch.n_own) store_node(A, A.u_cur, A.v_cur, g, u, v, a, hit, false);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      sx[k * L + l] = P.local_x0[(size_t)k * P.Lt + lb] + (float)u[k];
+      sd[k * L + l] = ep.dt * (float)v[k];
+      sa[k * L + l] = 0.f;
+    }
+  }
+  __syncthreads();
+
+  // -- elements, colour-ordered accumulation (as k_elem) ------------------------------
+  DevState S;
+  S.sig_a = A.sig_a;
+  S.sig_b = A.sig_b;
+  S.epbar = A.epbar;
+  S.status = A.status;
+  float wint = 0.f, wp = 0.f, vol = 0.f;
+  const int E = P.E;
+  for (int w = ch.elem_begin; w < ch.elem_end; w += BS) {
+    const int e = w + threadIdx.x;
+    const bool act = e < ch.elem_end;
+    int col = -1;
+    int ln[NPE];
+    float f[NPE][3];
+    if (act) {
+      col = P.color[e];
+      float x[NPE][3], du[NPE][3];
+#pragma unroll
+      for (int a = 0; a < NPE; a++) {
+        ln[a] = P.conn_local[(size_t)a * E + e];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          x[a][k] = sx[k * L + ln[a]];
+          du[a][k] = sd[k * L + ln[a]];
+        }
+      }
+      element_force<NPE, MODE>(ep, S, e, E, x, du, f, wint, wp, vol);
+    }
+    const int c0 = P.color[w];
+    const int c1 = P.color[min(w + BS, ch.elem_end) - 1];
+    for (int k = c0; k <= c1; k++) {
+      __syncthreads();
+      if (col == k) {
+#pragma unroll
+        for (int a = 0; a < NPE; a++) {
+          sa[ln[a]] += f[a][0];
+          sa[L + ln[a]] += f[a][1];
+          sa[2 * L + ln[a]] += f[a][2];
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // -- epilogue: interior nodes S^n -> S^{n+1}; boundary partials to the halo ---------
+#pragma unroll 2
+  for (int l = threadIdx.x; l < L; l += BS) {
+    if (l < ch.n_int) {
+      const int g = ch.own_begin + l;
+      double u[3], v[3], a[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        u[k] = A.u_cur[k][g];
+        v[k] = A.v_cur[k][g];
+      }
+      bool hit;
+      node_step(np, sa[l], sa[L + l], sa[2 * L + l], A.mass[g], A.d0[g], u, v, a, hit);
+      store_node(A, A.u_prv, A.v_prv, g, u, v, a, hit, A.store_acc != 0);
+    } else {
+      const int s = P.local_slot[ch.local_begin + l];
+      A.halo_cur[0][s] = sa[l];
+      A.halo_cur[1][s] = sa[L + l];
+      A.halo_cur[2][s] = sa[2 * L + l];
+    }
+  }
+  if (ep.accum_energy) {
+    const float t0 = block_sum<BS>(wint, red);
+    const float t1 = block_sum<BS>(wp, red);
+    if (threadIdx.x == 0) {
+      double* cw = A.chunk_work + 4 * (size_t)blockIdx.x;
+      cw[0] += (double)t0;
+      cw[1] += (double)t1;
+    }
+  }
+}
+
+// S^N of the boundary nodes after the last fused step of a call: reads S^{N-1} from
+// the prv buffer and the halo of step N-1, writes S^N (and a^N) to the cur buffer.
+__global__ void __launch_bounds__(256) k_finalize_boundary(FusedArgs A, NodeParams np,
+                                                           const int* bnd_nodes, int nb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const int g = bnd_nodes[i];
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  const int s1 = A.P.slot_row[g + 1];
+  for (int s = A.P.slot_row[g]; s < s1; s++) {
+    fx = __fadd_rn(fx, A.halo_prv[0][s]);
+    fy = __fadd_rn(fy, A.halo_prv[1][s]);
+    fz = __fadd_rn(fz, A.halo_prv[2][s]);
+  }
+  double u[3], v[3], a[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    u[k] = A.u_prv[k][g];
+    v[k] = A.v_prv[k][g];
+  }
+  bool hit;
+  node_step(np, fx, fy, fz, A.mass[g], A.d0[g], u, v, a, hit);
+  store_node(A, A.u_cur, A.v_cur, g, u, v, a, hit, true);
+}
+
 // Lumped mass: sum of the node's slots (component 0) in chunk order.
 __global__ void k_mass_sum(const float* slot_m, const int* slot_row, float* mass, int N) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;

@@ -85,7 +85,7 @@ bool build_plan(int N, int E, int npe, const double* xloc, const int* conn, int 
                                 : std::max(32, std::min(4096, (E + target_ctas - 1) / target_ctas));
   int lmax = chunk_nodes > 0 ? chunk_nodes : 2048;
   lmax = std::max(lmax, npe);
-  std::vector<int> stamp(N, -1), owner(N, -1);
+  std::vector<int> stamp(N, -1), owner(N, -1), touch(N, 0);
   std::vector<int> cbeg;  // chunk start in sfc order
   {
     int c = -1, ne = 0, nl = 0;
@@ -104,6 +104,7 @@ bool build_plan(int N, int E, int npe, const double* xloc, const int* conn, int 
         if (stamp[en[a]] != c) {
           stamp[en[a]] = c;
           nl++;
+          touch[en[a]]++;
           if (owner[en[a]] < 0) owner[en[a]] = c;
         }
       ne++;
@@ -114,22 +115,26 @@ bool build_plan(int N, int E, int npe, const double* xloc, const int* conn, int 
   P.n_chunks = C;
   P.chunks.resize(C);
 
-  // -- 3. node renumbering: owned nodes contiguous per chunk, first-touch order -------
+  // -- 3. node renumbering: owned nodes contiguous per chunk, interior ones first,
+  //       each group in first-touch order -----------------------------------------
   P.node_new.assign(N, -1);
   P.node_orig.assign(N, -1);
   int next = 0;
   for (int c = 0; c < C; c++) {
     P.chunks[c].own_begin = next;
-    for (int i = cbeg[c]; i < cbeg[c + 1]; i++) {
-      const int* en = conn + (size_t)npe * sfc[i];
-      for (int a = 0; a < npe; a++) {
-        const int n = en[a];
-        if (owner[n] == c && P.node_new[n] < 0) {
-          P.node_new[n] = next;
-          P.node_orig[next] = n;
-          next++;
+    for (int pass = 0; pass < 2; pass++) {
+      for (int i = cbeg[c]; i < cbeg[c + 1]; i++) {
+        const int* en = conn + (size_t)npe * sfc[i];
+        for (int a = 0; a < npe; a++) {
+          const int n = en[a];
+          if (owner[n] == c && P.node_new[n] < 0 && (pass == 0) == (touch[n] == 1)) {
+            P.node_new[n] = next;
+            P.node_orig[next] = n;
+            next++;
+          }
         }
       }
+      if (pass == 0) P.chunks[c].n_int = next - P.chunks[c].own_begin;
     }
     P.chunks[c].n_own = next - P.chunks[c].own_begin;
   }
@@ -261,6 +266,10 @@ bool verify_plan(const Plan& P, const int* conn, std::string* err) {
       const int s = P.local_slot[ch.local_begin + l];
       if (l < ch.n_own && gn != ch.own_begin + l) {
         *err = "owned local node does not map to the owned range";
+        return false;
+      }
+      if ((l < ch.n_int) != (P.slot_row[gn + 1] - P.slot_row[gn] == 1)) {
+        *err = "interior/boundary split does not match the slot counts";
         return false;
       }
       if (s < P.slot_row[gn] || s >= P.slot_row[gn + 1]) {

@@ -7,7 +7,9 @@
 //  * elements are sorted along a 3D Hilbert curve of their centroids and cut into
 //    contiguous CHUNKS; one CTA processes one chunk;
 //  * every node is OWNED by the first chunk that touches it, and nodes are renumbered
-//    so each chunk's owned nodes are contiguous (first-touch order along the curve);
+//    so each chunk's owned nodes are contiguous: first its INTERIOR nodes (touched by
+//    no other chunk), then its owned BOUNDARY nodes, each in first-touch order along
+//    the curve; the other chunks touching a boundary node hold it as a GHOST;
 //  * inside a chunk the elements are greedily coloured (no two elements of a colour
 //    share a node) and sorted by colour, so the CTA adds element forces into its
 //    shared-memory node accumulators colour by colour with plain read-modify-writes;
@@ -29,7 +31,8 @@ struct ChunkInfo {
   int n_own;        // owned nodes are local ids [0, n_own)
   int n_local;      // owned + ghost
   int local_begin;  // offset of this chunk's entries in the local tables
-  int pad0, pad1;
+  int n_int;        // interior nodes (touched by this chunk only) are local ids [0, n_int)
+  int pad;
 };
 
 struct Plan {

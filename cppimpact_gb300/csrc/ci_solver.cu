@@ -84,8 +84,13 @@ struct ci_solver {
   DBuf<uint8_t> d_color;
   DBuf<int> d_lgid, d_lslot, d_slot_row;
   DBuf<float> d_lx0;  // [3][Lt]
-  // state
+  // state (A buffer = d_u/d_v always holds the state between calls; B is the fused
+  // path's second buffer)
   DBuf<double> d_u, d_v;   // [3][N]
+  DBuf<double> d_ub, d_vb; // [3][N]
+  DBuf<float> d_halo1;     // [3][S] second halo buffer of the fused path
+  DBuf<int> d_bnd;         // boundary nodes (plan ids)
+  int n_bnd = 0;
   DBuf<float> d_slot;      // [3][S]
   DBuf<float> d_mass;      // [N]
   DBuf<double> d_d0;       // [N]
@@ -161,6 +166,35 @@ struct ci_solver {
     A.status = d_status.p;
     return A;
   }
+  ci::FusedArgs fused_args(bool cur_is_a, int halo_cur, bool bnd_final, bool store_acc) const {
+    ci::FusedArgs F;
+    F.P = dev_plan();
+    double* ua = d_u.p;
+    double* va = d_v.p;
+    double* ub = d_ub.p;
+    double* vb = d_vb.p;
+    float* h[2] = {d_slot.p, d_halo1.p};
+    for (int k = 0; k < 3; k++) {
+      F.u_cur[k] = (cur_is_a ? ua : ub) + (size_t)k * N;
+      F.v_cur[k] = (cur_is_a ? va : vb) + (size_t)k * N;
+      F.u_prv[k] = (cur_is_a ? ub : ua) + (size_t)k * N;
+      F.v_prv[k] = (cur_is_a ? vb : va) + (size_t)k * N;
+      F.halo_cur[k] = h[halo_cur] + (size_t)k * S;
+      F.halo_prv[k] = h[halo_cur ^ 1] + (size_t)k * S;
+      F.acc[k] = d_acc.p + (size_t)k * N;
+    }
+    F.mass = d_mass.p;
+    F.d0 = d_d0.p;
+    F.contact = d_contact.p;
+    F.sig_a = d_sig_a.p;
+    F.sig_b = d_sig_b.p;
+    F.epbar = d_epbar.p;
+    F.chunk_work = d_work.p;
+    F.status = d_status.p;
+    F.bnd_final = bnd_final ? 1 : 0;
+    F.store_acc = store_acc ? 1 : 0;
+    return F;
+  }
   ci::NodeParams node_params() const {
     ci::NodeParams p;
     p.dt = dt;
@@ -182,6 +216,15 @@ cudaError_t launch_elem(ci_solver* s, const ci::DevState& D, const ci::ElemParam
   return cudaGetLastError();
 }
 
+template <int NPE, int BS>
+cudaError_t configure_step(int bytes) {
+  cudaError_t e = cudaFuncSetAttribute(ci::k_step<NPE, ci::EM_J2, BS>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e) return e;
+  return cudaFuncSetAttribute(ci::k_step<NPE, ci::EM_REFCOMPAT, BS>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 // Raise the dynamic shared-memory limit of the element kernels once per solver (not
 // inside stream capture).
 template <int NPE>
@@ -196,8 +239,61 @@ cudaError_t configure_npe(int bytes) {
   if ((e = cudaFuncSetAttribute(ci::k_elem<NPE, ci::EM_MASS_ROWSUM, kBS>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
     return e;
+  if ((e = configure_step<NPE, 64>(bytes))) return e;
+  if ((e = configure_step<NPE, 128>(bytes))) return e;
+  if ((e = configure_step<NPE, 256>(bytes))) return e;
   return cudaFuncSetAttribute(ci::k_elem<NPE, ci::EM_MASS_HRZ, kBS>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+template <int NPE, int BS>
+cudaError_t launch_fused_bs(ci_solver* s, const ci::FusedArgs& F, const ci::ElemParams& ep,
+                            const ci::NodeParams& np) {
+  if (s->opt.mode != CI_MODE_REFCOMPAT)
+    ci::k_step<NPE, ci::EM_J2, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
+  else
+    ci::k_step<NPE, ci::EM_REFCOMPAT, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fused(ci_solver* s, const ci::FusedArgs& F) {
+  const ci::ElemParams ep = s->elem_params((float)s->dt, true);
+  const ci::NodeParams np = s->node_params();
+  const int bs = s->opt.block_threads;
+  if (s->npe == 4) {
+    if (bs == 64) return launch_fused_bs<4, 64>(s, F, ep, np);
+    if (bs == 128) return launch_fused_bs<4, 128>(s, F, ep, np);
+    return launch_fused_bs<4, 256>(s, F, ep, np);
+  }
+  if (bs == 64) return launch_fused_bs<10, 64>(s, F, ep, np);
+  if (bs == 128) return launch_fused_bs<10, 128>(s, F, ep, np);
+  return launch_fused_bs<10, 256>(s, F, ep, np);
+}
+
+cudaError_t launch_finalize(ci_solver* s, const ci::FusedArgs& F) {
+  if (s->n_bnd == 0) return cudaSuccess;
+  ci::k_finalize_boundary<<<(s->n_bnd + 255) / 256, 256, 0, s->stream>>>(F, s->node_params(),
+                                                                         s->d_bnd.p, s->n_bnd);
+  return cudaGetLastError();
+}
+
+// n fused steps from the state in buffer A, ending with the state in buffer A.
+cudaError_t enqueue_fused(ci_solver* s, int n, bool store_acc_last) {
+  if (n <= 0) return cudaSuccess;
+  cudaError_t e;
+  for (int i = 0; i < n; i++) {
+    const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0, store_acc_last && i == n - 1);
+    if ((e = launch_fused(s, F))) return e;
+  }
+  // boundary nodes: S^n from S^{n-1} (prv) and the halo of step n-1
+  const ci::FusedArgs F = s->fused_args((n & 1) == 0, n & 1, false, true);
+  if ((e = launch_finalize(s, F))) return e;
+  if (n & 1) {
+    const size_t b = sizeof(double) * 3 * (size_t)s->N;
+    if ((e = cudaMemcpyAsync(s->d_u.p, s->d_ub.p, b, cudaMemcpyDeviceToDevice, s->stream))) return e;
+    if ((e = cudaMemcpyAsync(s->d_v.p, s->d_vb.p, b, cudaMemcpyDeviceToDevice, s->stream))) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_elem_mode(ci_solver* s, int mode, const ci::DevState& D, const ci::ElemParams& p) {
@@ -272,7 +368,8 @@ int upload_reference(ci_solver* s) {
   return CI_OK;
 }
 
-int reset_state(ci_solver* s) {
+// u = 0 and v = the initial velocity everywhere.
+int reset_kinematics(ci_solver* s) {
   const int N = s->N;
   std::vector<double> v(3 * (size_t)N);
   for (int i = 0; i < N; i++)
@@ -280,6 +377,13 @@ int reset_state(ci_solver* s) {
   CI_CUDA(cudaMemsetAsync(s->d_u.p, 0, sizeof(double) * 3 * N, s->stream));
   CI_CUDA(cudaMemcpyAsync(s->d_v.p, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice,
                           s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  return CI_OK;
+}
+
+// Stored stress, plastic strain, contact history, work sums and status cleared.
+int reset_history(ci_solver* s) {
+  const int N = s->N;
   if (s->d_sig_a.p) {
     CI_CUDA(cudaMemsetAsync(s->d_sig_a.p, 0, sizeof(float4) * s->d_sig_a.n, s->stream));
     CI_CUDA(cudaMemsetAsync(s->d_sig_b.p, 0, sizeof(float2) * s->d_sig_b.n, s->stream));
@@ -293,6 +397,11 @@ int reset_state(ci_solver* s) {
   s->started = false;
   s->steps_done = 0;
   return CI_OK;
+}
+
+int reset_state(ci_solver* s) {
+  const int rc = reset_kinematics(s);
+  return rc ? rc : reset_history(s);
 }
 
 int compute_mass(ci_solver* s) {
@@ -311,12 +420,17 @@ void destroy_graph(ci_solver* s) {
   s->graph_steps = 0;
 }
 
+bool fused_path(const ci_solver* s) { return s->opt.step_kernel == 0; }
+
 int build_graph(ci_solver* s, int steps) {
   destroy_graph(s);
   cudaGraph_t g = nullptr;
   CI_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
-  for (int i = 0; i < steps && err == cudaSuccess; i++) err = enqueue_step(s, false);
+  if (fused_path(s))
+    err = enqueue_fused(s, steps, false);
+  else
+    for (int i = 0; i < steps && err == cudaSuccess; i++) err = enqueue_step(s, false);
   cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
   if (err != cudaSuccess) return fail(CI_ERR_CUDA, "graph capture: %s", cudaGetErrorString(err));
   if (e2 != cudaSuccess) return fail(CI_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e2));
@@ -330,6 +444,24 @@ int build_graph(ci_solver* s, int steps) {
 // Enqueue n steps; the last stores the acceleration for energy read-back.
 int enqueue_steps(ci_solver* s, int n) {
   if (n <= 0) return CI_OK;
+  if (fused_path(s)) {
+    // graphs of G (even) steps + boundary finalize, then the remainder directly
+    const int G = (s->opt.graph_steps > 0 ? s->opt.graph_steps : 32) & ~1;
+    int rest = n;
+    if (G >= 2 && rest > G) {
+      if (!s->graph || s->graph_steps != G) {
+        const int rc = build_graph(s, G);
+        if (rc) return rc;
+      }
+      while (rest > G) {
+        CI_CUDA(cudaGraphLaunch(s->graph, s->stream));
+        rest -= G;
+      }
+    }
+    CI_CUDA(enqueue_fused(s, rest, true));
+    s->steps_done += n;
+    return CI_OK;
+  }
   const int G = s->opt.graph_steps > 0 ? s->opt.graph_steps : 32;
   int rest = n - 1;
   if (rest >= G) {
@@ -395,6 +527,11 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
     ci_default_options(&s->opt);
   if (s->opt.mode != CI_MODE_J2 && s->opt.mode != CI_MODE_REFCOMPAT)
     return fail(CI_ERR_INVALID, "unknown mode");
+  if (s->opt.step_kernel != 0 && s->opt.step_kernel != 1)
+    return fail(CI_ERR_INVALID, "unknown step_kernel");
+  if (s->opt.block_threads == 0) s->opt.block_threads = 128;
+  if (s->opt.block_threads != 64 && s->opt.block_threads != 128 && s->opt.block_threads != 256)
+    return fail(CI_ERR_INVALID, "block_threads must be 64, 128 or 256");
   s->mat = *mat;
   s->wall = *wall;
   s->N = mesh->num_nodes;
@@ -438,6 +575,16 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   CI_CUDA(s->d_u.alloc(3 * N));
   CI_CUDA(s->d_v.alloc(3 * N));
   CI_CUDA(s->d_slot.alloc(3 * (size_t)s->S));
+  if (s->opt.step_kernel == 0) {
+    CI_CUDA(s->d_ub.alloc(3 * N));
+    CI_CUDA(s->d_vb.alloc(3 * N));
+    CI_CUDA(s->d_halo1.alloc(3 * (size_t)s->S));
+    std::vector<int> bnd;
+    for (int n = 0; n < s->N; n++)
+      if (P.slot_row[n + 1] - P.slot_row[n] > 1) bnd.push_back(n);
+    s->n_bnd = (int)bnd.size();
+    if ((rc = upload(s->d_bnd, bnd, s->stream))) return rc;
+  }
   CI_CUDA(s->d_mass.alloc(N));
   CI_CUDA(s->d_d0.alloc(N));
   CI_CUDA(s->d_contact.alloc(N));
@@ -482,7 +629,7 @@ int ci_start(ci_solver* s, double dt) {
   if (!s) return fail(CI_ERR_INVALID, "null solver");
   if (!(dt > 0.0)) return fail(CI_ERR_INVALID, "dt must be positive");
   CI_CUDA(cudaSetDevice(s->device));
-  int rc = reset_state(s);
+  int rc = reset_history(s);
   if (rc) return rc;
   s->dt = dt;
   destroy_graph(s);
@@ -827,24 +974,51 @@ int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms) {
   CI_CUDA(cudaSetDevice(s->device));
   std::vector<cudaEvent_t> ev(3 * nsteps);
   for (auto& e : ev) CI_CUDA(cudaEventCreate(&e));
-  const ci::DevState D = s->dev_state(s->d_u.p, s->d_v.p);
-  const int nb = (s->N + 255) / 256;
-  for (int i = 0; i < nsteps; i++) {
-    CI_CUDA(cudaEventRecord(ev[3 * i], s->stream));
-    CI_CUDA(launch_elem_mode(s, step_mode(s), D, s->elem_params((float)s->dt, true)));
-    CI_CUDA(cudaEventRecord(ev[3 * i + 1], s->stream));
-    ci::k_node<false, true><<<nb, 256, 0, s->stream>>>(s->node_arrays(), s->node_params());
-    CI_CUDA(cudaGetLastError());
-    CI_CUDA(cudaEventRecord(ev[3 * i + 2], s->stream));
-  }
-  CI_CUDA(cudaEventSynchronize(ev.back()));
   double te = 0, tn = 0;
-  for (int i = 0; i < nsteps; i++) {
-    float a, b;
-    CI_CUDA(cudaEventElapsedTime(&a, ev[3 * i], ev[3 * i + 1]));
-    CI_CUDA(cudaEventElapsedTime(&b, ev[3 * i + 1], ev[3 * i + 2]));
-    te += a;
-    tn += b;
+  if (fused_path(s)) {
+    // out[0]: mean k_step duration; out[1]: the end-of-call boundary finalise
+    for (int i = 0; i < nsteps; i++) {
+      const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0, i == nsteps - 1);
+      CI_CUDA(cudaEventRecord(ev[3 * i], s->stream));
+      CI_CUDA(launch_fused(s, F));
+      CI_CUDA(cudaEventRecord(ev[3 * i + 1], s->stream));
+    }
+    const ci::FusedArgs F = s->fused_args((nsteps & 1) == 0, nsteps & 1, false, true);
+    CI_CUDA(launch_finalize(s, F));
+    CI_CUDA(cudaEventRecord(ev[2], s->stream));
+    if (nsteps & 1) {
+      const size_t b = sizeof(double) * 3 * (size_t)s->N;
+      CI_CUDA(cudaMemcpyAsync(s->d_u.p, s->d_ub.p, b, cudaMemcpyDeviceToDevice, s->stream));
+      CI_CUDA(cudaMemcpyAsync(s->d_v.p, s->d_vb.p, b, cudaMemcpyDeviceToDevice, s->stream));
+    }
+    CI_CUDA(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < nsteps; i++) {
+      float a;
+      CI_CUDA(cudaEventElapsedTime(&a, ev[3 * i], ev[3 * i + 1]));
+      te += a;
+    }
+    float b;
+    CI_CUDA(cudaEventElapsedTime(&b, ev[3 * (nsteps - 1) + 1], ev[2]));
+    tn = b * nsteps;
+  } else {
+    const ci::DevState D = s->dev_state(s->d_u.p, s->d_v.p);
+    const int nb = (s->N + 255) / 256;
+    for (int i = 0; i < nsteps; i++) {
+      CI_CUDA(cudaEventRecord(ev[3 * i], s->stream));
+      CI_CUDA(launch_elem_mode(s, step_mode(s), D, s->elem_params((float)s->dt, true)));
+      CI_CUDA(cudaEventRecord(ev[3 * i + 1], s->stream));
+      ci::k_node<false, true><<<nb, 256, 0, s->stream>>>(s->node_arrays(), s->node_params());
+      CI_CUDA(cudaGetLastError());
+      CI_CUDA(cudaEventRecord(ev[3 * i + 2], s->stream));
+    }
+    CI_CUDA(cudaEventSynchronize(ev.back()));
+    for (int i = 0; i < nsteps; i++) {
+      float a, b;
+      CI_CUDA(cudaEventElapsedTime(&a, ev[3 * i], ev[3 * i + 1]));
+      CI_CUDA(cudaEventElapsedTime(&b, ev[3 * i + 1], ev[3 * i + 2]));
+      te += a;
+      tn += b;
+    }
   }
   for (auto& e : ev) cudaEventDestroy(e);
   s->steps_done += nsteps;
@@ -853,7 +1027,7 @@ int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms) {
   return check_status(s);
 }
 
-int ci_launches_per_step(const ci_solver* s) { return s ? 2 : 0; }
+int ci_launches_per_step(const ci_solver* s) { return s ? (s->opt.step_kernel == 0 ? 1 : 2) : 0; }
 
 int ci_plan_stats(const ci_mesh* mesh, int chunk_elements, int chunk_nodes, long long* stats,
                   int* perm_elems, int* perm_nodes) {

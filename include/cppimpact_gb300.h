@@ -94,6 +94,8 @@ typedef struct ci_options {
   int chunk_elements; /* elements per CTA chunk, 0 = automatic */
   int chunk_nodes;    /* local-node budget per chunk, 0 = automatic */
   int graph_steps;    /* steps captured per CUDA graph, 0 = automatic */
+  int step_kernel;    /* 0 = fused (one launch per step, default), 1 = element + node kernels */
+  int block_threads;  /* threads per chunk CTA of the fused kernel: 64, 128 or 256; 0 = automatic */
 } ci_options;
 
 /* energy terms (FP64), see ci_get_energy */
@@ -123,14 +125,16 @@ int ci_destroy(ci_solver* s);
  * stored stress and plastic strain zero, contact history cleared. */
 int ci_initialize(ci_solver* s, const double pos[3], const double vel[3]);
 
-/* Dynamics::solve (include/dynamics.h:414-512): lumped mass, a0 from zero increment,
- * v += dt/2 a0, then steps while time <= time_end (time += dt in double, the
- * reference's loop count).  export_interval is accepted for signature parity; state
- * is read back with ci_get_state. */
+/* Dynamics::solve (include/dynamics.h:414-512): ci_start (lumped mass, a0 from zero
+ * increment, v += dt/2 a0) then steps while time <= time_end (time += dt in double,
+ * the reference's loop count).  export_interval is accepted for signature parity;
+ * state is read back with ci_get_state. */
 int ci_solve(ci_solver* s, double dt, double time_end, int export_interval);
 
-/* Lower-level stepping: ci_start does the mass, a0 and half step of Dynamics::solve;
- * ci_step advances nsteps more steps of size dt (graph-captured). */
+/* Lower-level stepping: ci_start does the mass, a0 and half step of Dynamics::solve
+ * from the current positions and velocities (those of ci_initialize or ci_set_state)
+ * and clears the stored stress, plastic strain and contact history; ci_step advances
+ * nsteps more steps of size dt (graph-captured). */
 int ci_start(ci_solver* s, double dt);
 int ci_step(ci_solver* s, int nsteps);
 int ci_steps_done(const ci_solver* s, long long* nsteps);
@@ -163,8 +167,10 @@ int ci_strain_energy(ci_solver* s, const double* u, double* energy, double* volu
 
 /* ---- timing helpers for benchmarks (CUDA events on the solver's stream) ---- */
 int ci_time_steps(ci_solver* s, int nsteps, float* ms);
-/* Mean device duration (ms) of each kernel kind over the last ci_time_kernels call:
- * out[0] element kernel, out[1] node kernel. */
+/* Runs nsteps steps launching each kernel between CUDA events and returns mean device
+ * durations (ms): fused path out[0] = the step kernel, out[1] = the end-of-call
+ * boundary finalise divided by nsteps; two-kernel path out[0] = element kernel,
+ * out[1] = node kernel. */
 int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms);
 /* Kernel launches one step issues (for launch accounting). */
 int ci_launches_per_step(const ci_solver* s);

@@ -1,0 +1,95 @@
+"""The C++ drop-in headers (include/cppimpact/) keep the reference's class names and
+signatures: the reference's own drivers compile unchanged against them and link to
+libcppimpact_gb300.so.  A driver written in the reference's style runs on the GPU
+(marked gpu)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from cppimpact_gb300 import meshgen as mg
+
+REF = "/root/reference"
+INC = os.path.join(ROOT, "include", "cppimpact")
+LIBDIR = os.path.join(ROOT, "cppimpact_gb300")
+STUB = os.path.join(ROOT, "oracle", "stub")
+
+
+def _compile(src_text, tmp, name, defines=()):
+    """Compile a driver that includes "include/<header>.h" with include/ -> drop-in headers."""
+    work = tmp / name
+    work.mkdir()
+    os.symlink(INC, work / "include")
+    (work / "driver.cpp").write_text(src_text)
+    exe = work / "driver"
+    cmd = ["g++", "-std=c++17", "-O1", *[f"-D{d}" for d in defines], f"-I{STUB}", f"-I{work}",
+           str(work / "driver.cpp"), f"-L{LIBDIR}", "-lcppimpact_gb300",
+           f"-Wl,-rpath,{LIBDIR}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference checkout not present")
+@pytest.mark.parametrize("driver,defines", [("test.cu", ()), ("FEA_debug.cu", ("USE_LINEAR_BASIS",)),
+                                            ("FEA_debug.cu", ("USE_QUADRATIC_BASIS",))])
+def test_reference_drivers_compile_unchanged(cilib, tmp_path, driver, defines):
+    src = open(os.path.join(REF, driver)).read()
+    _compile(src, tmp_path, driver.replace(".", "_") + "_".join(defines), defines)
+
+
+DRIVER = r'''
+#include <cstdio>
+#include "include/analysis.h"
+#include "include/elastoplastic.h"
+#include "include/wall.h"
+#include "include/dynamics.h"
+int main(int argc, char** argv) {
+  Mesh<T, Basis::nodes_per_element> mesh;
+  if (mesh.load_mesh(argv[1]) != 0) return 1;
+  Elastoplastic<T, 3> material(68.9e9, 2700, 0.33, 0.0, 0.689e9, 276e6, "AL6061");
+  Wall<T, 2, Basis> w("Wall", atof(argv[2]), atof(argv[3]), mesh.slave_nodes, mesh.num_slave_nodes, 1);
+  Dynamics<T, Basis, Analysis, Quadrature> dyna(&mesh, &material, &w);
+  dyna.output_dir = argv[5];
+  T pos[] = {0, 0, 0}, vel[] = {0, 0, -10};
+  dyna.initialize(pos, vel);
+  const double dt = atof(argv[4]);
+  dyna.solve(dt, 199 * dt + 0.5 * dt, 100);
+  FILE* f = fopen(argv[6], "wb");
+  fwrite(dyna.global_xloc, sizeof(double), dyna.ndof, f);
+  fwrite(dyna.vel, sizeof(double), dyna.ndof, f);
+  fclose(f);
+  dyna.debug_strain(0.01, 0);
+  printf("W %.17g V %.17g\n", dyna.last_strain_energy, dyna.last_volume);
+  return 0;
+}
+'''
+
+
+@pytest.mark.gpu
+def test_reference_style_driver_runs_on_gpu(cilib, oracle, tmp_path):
+    """A test.cu-style driver through the drop-in headers: 200 steps of the reference's
+    force law, VTK exports every 100 steps, matched against the restated reference."""
+    m = mg.cube(4, 1)
+    inp = tmp_path / "m.inp"
+    mg.write_inp(m, str(inp))
+    exe = _compile(DRIVER, tmp_path, "drv")
+    loc = float(m.xloc[:, 2].min()) - 1e-5
+    k, dt = 6.89e11, 1e-7
+    out = tmp_path / "out"
+    out.mkdir()
+    state = tmp_path / "state.f64"
+    r = subprocess.run([str(exe), str(inp), repr(loc), repr(k), repr(dt), str(out), str(state)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    xv = np.fromfile(state).reshape(2, -1, 3)
+    ref = oracle.ref_solve(m.xloc, m.conn, oracle.ref_params(68.9e9, 0.33, 2700.0, loc, k, 1),
+                           (0, 0, -10), dt, 199 * dt + 0.5 * dt)
+    u_ref = ref["x"].reshape(-1, 3) - m.xloc
+    assert np.linalg.norm(xv[0] - m.xloc - u_ref) < 1e-3 * np.linalg.norm(u_ref)
+    assert sorted(os.listdir(out)) == ["simulation_0.vtk", "simulation_100.vtk"]
+    W = float(r.stdout.split("W ")[1].split()[0])
+    assert W == pytest.approx(84161.61854712779, rel=1e-5)

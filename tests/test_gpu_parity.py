@@ -158,7 +158,7 @@ def test_refcompat_trajectory_vs_reference_tet4(cilib):
     assert rel(st["x"] - g["xloc"], g["x"] - g["xloc"]) < 1e-3
 
 
-@pytest.mark.parametrize("order,n,steps,speed", [(1, 6, 800, 10.0), (2, 3, 600, 20.0)])
+@pytest.mark.parametrize("order,n,steps,speed", [(1, 6, 800, 30.0), (2, 3, 600, 20.0)])
 def test_j2_trajectory_vs_fp64(cilib, oracle, order, n, steps, speed):
     m = mg.cube(n, order)
     setup = mg.impact_setup(m, speed, 1e-4)
@@ -225,3 +225,31 @@ def test_nonfinite_state_reported(cilib):
     with pytest.raises(cilib.CiError) as ei:
         s.start(1e-7)
     assert ei.value.code == -4
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_fused_step_split_invariance(cilib, order):
+    """The fused path finalises boundary nodes either at the start of the next step or
+    in the end-of-call kernel; both use the same rounding, so splitting a run into
+    calls of any length (graph-captured or not, odd or even) changes no bit."""
+    m = mg.cube(5, order)
+    setup = mg.impact_setup(m, 20.0, 1e-4)
+    a = _run_gpu(cilib, m, setup, cilib.MODE_J2, 0, graph_steps=8)
+    a.step(77)
+    b = _run_gpu(cilib, m, setup, cilib.MODE_J2, 0, graph_steps=8)
+    for n in (1, 2, 9, 16, 17, 32):
+        b.step(n)
+    sa, sb = a.state(), b.state()
+    for k in ("x", "v", "sigma", "epbar", "contact"):
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_fused_matches_two_kernel_path(cilib, order):
+    m = mg.cube(5, order)
+    setup = mg.impact_setup(m, 20.0, 1e-4)
+    a = _run_gpu(cilib, m, setup, cilib.MODE_J2, 300).state()
+    b = _run_gpu(cilib, m, setup, cilib.MODE_J2, 300, step_kernel=1).state()
+    assert rel(a["x"] - m.xloc, b["x"] - m.xloc) < 1e-5
+    assert rel(a["epbar"], b["epbar"]) < 1e-4
+    assert np.array_equal(a["contact"] & 2, b["contact"] & 2)
