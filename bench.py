@@ -197,6 +197,7 @@ def run_ours(args, rank, world):
     s = api.Solver(m.xloc, m.conn, **MAT, mode=api.MODE_J2, lumping=api.LUMP_HRZ,
                    step_kernel=args.step_kernel, chunk_elements=args.chunk_elements,
                    chunk_nodes=args.chunk_nodes, block_threads=args.block_threads,
+                   elem_lanes=args.elem_lanes,
                    wall_normal=setup["wall_normal"], wall_offset=setup["wall_offset"],
                    wall_stiffness=setup["wall_stiffness"],
                    device=int(os.environ.get("LOCAL_RANK", "0")))
@@ -328,6 +329,7 @@ def main():
     ap.add_argument("--chunk-elements", type=int, default=0)
     ap.add_argument("--chunk-nodes", type=int, default=0)
     ap.add_argument("--block-threads", type=int, default=0)
+    ap.add_argument("--elem-lanes", type=int, default=0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-interval", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -55,7 +55,8 @@ class CiWall(C.Structure):
 class CiOptions(C.Structure):
     _fields_ = [("mode", C.c_int), ("lumping", C.c_int), ("gravity", C.c_double * 3),
                 ("device", C.c_int), ("chunk_elements", C.c_int), ("chunk_nodes", C.c_int),
-                ("graph_steps", C.c_int), ("step_kernel", C.c_int), ("block_threads", C.c_int)]
+                ("graph_steps", C.c_int), ("step_kernel", C.c_int), ("block_threads", C.c_int),
+                ("elem_lanes", C.c_int)]
 
 
 class CiEnergy(C.Structure):
@@ -174,7 +175,7 @@ class Solver:
                  wall_normal=(0.0, 0.0, 1.0), wall_offset=-1e30, wall_stiffness=0.0,
                  mode=MODE_J2, lumping=LUMP_HRZ, gravity=(0.0, 0.0, -9.81), device=0,
                  chunk_elements=0, chunk_nodes=0, graph_steps=0, step_kernel=0, block_threads=0,
-                 slave=None, fixed=None):
+                 elem_lanes=0, slave=None, fixed=None):
         self.mesh = MeshArrays(xloc, conn, slave, fixed)
         self.N, self.E = self.mesh.xloc.shape[0], self.mesh.conn.shape[0]
         self.npe = self.mesh.conn.shape[1]
@@ -182,7 +183,7 @@ class Solver:
         mat = CiMaterial(E, nu, rho, sigma_y0, H, beta)
         wall = CiWall((C.c_double * 3)(*wall_normal), wall_offset, wall_stiffness)
         opt = CiOptions(mode, lumping, (C.c_double * 3)(*gravity), device, chunk_elements,
-                        chunk_nodes, graph_steps, step_kernel, block_threads)
+                        chunk_nodes, graph_steps, step_kernel, block_threads, elem_lanes)
         self._h = C.c_void_p()
         check(lib().ci_create(C.byref(self.mesh.c), C.byref(mat), C.byref(wall), C.byref(opt),
                               C.byref(self._h)))

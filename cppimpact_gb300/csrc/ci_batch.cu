@@ -1,0 +1,600 @@
+// ci_batch.cu -- many impact instances of uneven size advanced by one launch per step.
+//
+// Each instance (mesh, material, wall, initial state, its own dt and end time) is
+// planned exactly as a single solve would plan it (ci_plan.cpp); the plans of all
+// instances with the same element type are concatenated into one plan whose chunks
+// carry their instance id.  The fused step kernel reads each chunk's parameters from
+// per-instance tables and the global step from a device counter, so a captured graph
+// of 32 steps can be replayed: an instance steps while step < nsteps, finalises its
+// boundary nodes at step == nsteps and idles afterwards.  tet4 and tet10 groups run on
+// two streams.  Because every instance runs the same kernels on the same plan as its
+// single solve, its result is bitwise that of the unbatched run (tests check it).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/cppimpact_gb300.h"
+#include "ci_kernels.cuh"
+#include "ci_plan.h"
+
+namespace ci {
+int set_last_error(int code, const char* msg);
+}
+using namespace ci;
+
+namespace {
+
+int fail(int code, const std::string& msg) { return ci::set_last_error(code, msg.c_str()); }
+
+#define CB_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(CI_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+  } while (0)
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t alloc(size_t count) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = count;
+    return count ? cudaMalloc(&p, sizeof(T) * count) : cudaSuccess;
+  }
+  template <typename V>
+  cudaError_t upload(const std::vector<V>& h, cudaStream_t st) {
+    cudaError_t e = alloc(h.size());
+    if (e || h.empty()) return e;
+    return cudaMemcpyAsync(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, st);
+  }
+};
+
+constexpr int kGraphSteps = 32;
+
+struct Inst {
+  int group = 0, index = 0;  // group (0 tet4, 1 tet10) and index within it
+  int N = 0, E = 0, npe = 0;
+  int node_off = 0, elem_off = 0;
+  int nsteps = 0;
+  double dt = 0.0;
+  std::vector<double> X;        // reference positions (mesh + pos), caller order
+  std::vector<int> node_orig;   // plan node -> caller node (instance-local)
+  std::vector<int> elem_orig;   // plan element -> caller element (instance-local)
+  ci_material mat;
+  ci_wall wall;
+  double vel[3];
+};
+
+struct Group {
+  int npe = 0, nq = 0;
+  int N = 0, E = 0, C = 0, n_bnd = 0;
+  long long S = 0, Lt = 0;
+  int max_local = 0;
+  size_t smem = 0;
+  int block_threads = 128, elem_lanes = 4, chunk_nodes = 2048;
+  std::vector<int> insts;  // global instance ids
+  int max_steps = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  DBuf<ChunkInfo> chunks;
+  DBuf<uint16_t> conn;
+  DBuf<uint8_t> color;
+  DBuf<int> lgid, lslot, slot_row, bnd, node_inst;
+  DBuf<float> lx0, slot0, slot1, mass, d0f, acc, epbar, peak;
+  DBuf<double> ua, va, ub, vb, v0, d0, work;
+  DBuf<unsigned char> contact;
+  DBuf<float4> sig_a;
+  DBuf<float2> sig_b;
+  DBuf<unsigned int> status;
+  DBuf<ElemParams> inst_ep;
+  DBuf<NodeParams> inst_np;
+  DBuf<int> inst_nsteps, step_ctr;
+  ~Group() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+}  // namespace
+
+struct ci_batch {
+  int device = 0;
+  std::vector<Inst> inst;
+  std::unique_ptr<Group> g[2];
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_ms = 0.f;
+  bool done = false;
+  ~ci_batch() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+  }
+};
+
+namespace {
+
+ElemParams make_ep(const ci_material& m, double dt) {
+  ElemParams p{};
+  p.dt = (float)dt;
+  p.mu = (float)(m.E / (2.0 * (1.0 + m.nu)));
+  p.lambda = (float)(m.E * m.nu / ((1.0 + m.nu) * (1.0 - 2.0 * m.nu)));
+  const bool elastic = !(m.sigma_y0 > 0.0) || m.sigma_y0 > 1e30;
+  p.sy0 = elastic ? 3.0e38f : (float)m.sigma_y0;
+  p.H = (float)m.H;
+  p.rho = (float)m.rho;
+  p.accum_energy = 1;
+  return p;
+}
+
+NodeParams make_np(const ci_wall& w, const double gravity[3], double dt, int N) {
+  NodeParams p{};
+  p.dt = dt;
+  for (int k = 0; k < 3; k++) {
+    p.g[k] = gravity[k];
+    p.wall_n[k] = w.normal[k];
+    p.gf[k] = (float)gravity[k];
+    p.nf[k] = (float)w.normal[k];
+  }
+  p.wall_k = w.stiffness;
+  p.N = N;
+  return p;
+}
+
+FusedArgs group_args(const Group& G, int i_in_graph) {
+  FusedArgs F{};
+  F.P.chunks = G.chunks.p;
+  F.P.conn_local = G.conn.p;
+  F.P.color = G.color.p;
+  F.P.local_gid = G.lgid.p;
+  F.P.local_slot = G.lslot.p;
+  F.P.local_x0 = G.lx0.p;
+  F.P.slot_row = G.slot_row.p;
+  F.P.E = G.E;
+  F.P.N = G.N;
+  F.P.Lt = (int)G.Lt;
+  const bool even = (i_in_graph & 1) == 0;
+  const size_t N = G.N, S = G.S;
+  for (int k = 0; k < 3; k++) {
+    F.u_cur[k] = (even ? G.ua.p : G.ub.p) + k * N;
+    F.v_cur[k] = (even ? G.va.p : G.vb.p) + k * N;
+    F.u_prv[k] = (even ? G.ub.p : G.ua.p) + k * N;
+    F.v_prv[k] = (even ? G.vb.p : G.va.p) + k * N;
+    F.halo_cur[k] = (even ? G.slot0.p : G.slot1.p) + k * S;
+    F.halo_prv[k] = (even ? G.slot1.p : G.slot0.p) + k * S;
+    F.acc[k] = G.acc.p + k * N;
+  }
+  F.mass = G.mass.p;
+  F.d0 = G.d0.p;
+  F.d0f = G.d0f.p;
+  F.contact = G.contact.p;
+  F.sig_a = G.sig_a.p;
+  F.sig_b = G.sig_b.p;
+  F.epbar = G.epbar.p;
+  F.chunk_work = G.work.p;
+  F.status = G.status.p;
+  F.bnd_final = 0;
+  F.store_acc = 0;
+  F.inst_ep = G.inst_ep.p;
+  F.inst_np = G.inst_np.p;
+  F.inst_nsteps = G.inst_nsteps.p;
+  F.step_ctr = G.step_ctr.p;
+  F.step_off = i_in_graph;
+  return F;
+}
+
+template <int NPE, int BS>
+cudaError_t launch_batch_bs(Group& G, const FusedArgs& F) {
+  const ElemParams ep{};
+  const NodeParams np{};
+  if (NPE == 10 && G.elem_lanes == 4)
+    k_step_qp10<EM_J2, BS, true><<<G.C, BS, G.smem, G.stream>>>(F, ep, np);
+  else
+    k_step<NPE, EM_J2, BS, true><<<G.C, BS, G.smem, G.stream>>>(F, ep, np);
+  return cudaGetLastError();
+}
+
+template <int NPE>
+cudaError_t launch_batch(Group& G, const FusedArgs& F) {
+  if (G.block_threads == 64) return launch_batch_bs<NPE, 64>(G, F);
+  if (G.block_threads == 256) return launch_batch_bs<NPE, 256>(G, F);
+  return launch_batch_bs<NPE, 128>(G, F);
+}
+
+template <int NPE, int BS>
+cudaError_t configure_bs(int bytes) {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_step<NPE, EM_J2, BS, true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+    return e;
+  if (NPE == 10)
+    if ((e = cudaFuncSetAttribute(k_step_qp10<EM_J2, BS, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+      return e;
+  return cudaFuncSetAttribute(k_elem<NPE, EM_MASS_HRZ, 256>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+template <int NPE>
+cudaError_t configure(int bytes) {
+  cudaError_t e;
+  if ((e = configure_bs<NPE, 64>(bytes))) return e;
+  if ((e = configure_bs<NPE, 128>(bytes))) return e;
+  if ((e = configure_bs<NPE, 256>(bytes))) return e;
+  return cudaFuncSetAttribute(k_elem<NPE, EM_MASS_ROWSUM, 256>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+// Build one element-type group from its instances.
+int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& opt) {
+  std::vector<Plan> plans(G.insts.size());
+  std::string err;
+  for (size_t j = 0; j < G.insts.size(); j++) {
+    const ci_instance& I = in[G.insts[j]];
+    if (!build_plan(I.mesh.num_nodes, I.mesh.num_elements, I.mesh.nodes_per_element, I.mesh.xloc,
+                    I.mesh.element_nodes, opt.chunk_elements, G.chunk_nodes, 304, &plans[j], &err))
+      return fail(CI_ERR_INVALID, "instance " + std::to_string(G.insts[j]) + ": " + err);
+  }
+  // sizes and offsets
+  G.N = G.E = G.C = 0;
+  G.S = G.Lt = 0;
+  G.max_local = 0;
+  for (size_t j = 0; j < plans.size(); j++) {
+    Inst& T = b->inst[G.insts[j]];
+    T.node_off = G.N;
+    T.elem_off = G.E;
+    T.node_orig = plans[j].node_orig;
+    T.elem_orig = plans[j].elem_orig;
+    G.N += plans[j].N;
+    G.E += plans[j].E;
+    G.C += plans[j].n_chunks;
+    G.S += plans[j].slot_row[plans[j].N];
+    G.Lt += (long long)plans[j].local_gid.size();
+    G.max_local = std::max(G.max_local, plans[j].max_local);
+  }
+  const int npe = G.npe;
+  std::vector<ChunkInfo> chunks;
+  std::vector<uint16_t> conn((size_t)npe * G.E);
+  std::vector<uint8_t> color;
+  std::vector<int> lgid, lslot, slot_row, bnd, node_inst;
+  std::vector<float> lx0(3 * (size_t)G.Lt), d0f;
+  std::vector<double> d0, v0(3 * (size_t)G.N);
+  std::vector<ElemParams> eps;
+  std::vector<NodeParams> nps;
+  std::vector<int> nsteps;
+  long long s_off = 0, l_off = 0;
+  slot_row.reserve(G.N + 1);
+  G.max_steps = 0;
+  for (size_t j = 0; j < plans.size(); j++) {
+    const Plan& P = plans[j];
+    Inst& T = b->inst[G.insts[j]];
+    for (ChunkInfo c : P.chunks) {
+      c.elem_begin += T.elem_off;
+      c.elem_end += T.elem_off;
+      c.own_begin += T.node_off;
+      c.local_begin += (int)l_off;
+      c.inst = (int)j;
+      chunks.push_back(c);
+    }
+    for (int a = 0; a < npe; a++)
+      std::memcpy(&conn[(size_t)a * G.E + T.elem_off], &P.conn_local[(size_t)a * P.E],
+                  sizeof(uint16_t) * P.E);
+    color.insert(color.end(), P.color.begin(), P.color.end());
+    for (size_t l = 0; l < P.local_gid.size(); l++) {
+      lgid.push_back(P.local_gid[l] + T.node_off);
+      lslot.push_back(P.local_slot[l] + (int)s_off);
+    }
+    for (int n = 0; n < P.N; n++) {
+      slot_row.push_back(P.slot_row[n] + (int)s_off);
+      if (P.slot_row[n + 1] - P.slot_row[n] > 1) bnd.push_back(n + T.node_off);
+      node_inst.push_back((int)j);
+      const int o = P.node_orig[n];
+      const double* x = &T.X[3 * (size_t)o];
+      const double d = T.wall.normal[0] * x[0] + T.wall.normal[1] * x[1] +
+                       T.wall.normal[2] * x[2] - T.wall.offset;
+      d0.push_back(d);
+      d0f.push_back((float)d);
+      for (int k = 0; k < 3; k++) v0[(size_t)k * G.N + T.node_off + n] = T.vel[k];
+    }
+    // chunk-relative reference coordinates
+    for (int c = 0; c < P.n_chunks; c++) {
+      const ChunkInfo& ch = P.chunks[c];
+      const int o = P.node_orig[P.local_gid[ch.local_begin]];
+      for (int l = 0; l < ch.n_local; l++) {
+        const int lb = ch.local_begin + l;
+        const int n = P.node_orig[P.local_gid[lb]];
+        for (int k = 0; k < 3; k++)
+          lx0[(size_t)k * G.Lt + l_off + lb] = (float)(T.X[3 * (size_t)n + k] - T.X[3 * (size_t)o + k]);
+      }
+    }
+    s_off += P.slot_row[P.N];
+    l_off += (long long)P.local_gid.size();
+    eps.push_back(make_ep(T.mat, T.dt));
+    nps.push_back(make_np(T.wall, opt.gravity, T.dt, P.N));
+    nsteps.push_back(T.nsteps);
+    G.max_steps = std::max(G.max_steps, T.nsteps);
+  }
+  slot_row.push_back((int)s_off);
+  G.n_bnd = (int)bnd.size();
+  G.smem = sizeof(float) * 9 * (size_t)G.max_local;
+  cudaStream_t st = G.stream;
+  CB_CUDA(G.chunks.upload(chunks, st));
+  CB_CUDA(G.conn.upload(conn, st));
+  CB_CUDA(G.color.upload(color, st));
+  CB_CUDA(G.lgid.upload(lgid, st));
+  CB_CUDA(G.lslot.upload(lslot, st));
+  CB_CUDA(G.slot_row.upload(slot_row, st));
+  CB_CUDA(G.bnd.upload(bnd, st));
+  CB_CUDA(G.node_inst.upload(node_inst, st));
+  CB_CUDA(G.lx0.upload(lx0, st));
+  CB_CUDA(G.d0.upload(d0, st));
+  CB_CUDA(G.d0f.upload(d0f, st));
+  CB_CUDA(G.inst_ep.upload(eps, st));
+  CB_CUDA(G.inst_np.upload(nps, st));
+  CB_CUDA(G.inst_nsteps.upload(nsteps, st));
+  CB_CUDA(G.v0.upload(v0, st));
+  CB_CUDA(G.va.alloc(3 * (size_t)G.N));
+  const size_t N = G.N, E = G.E;
+  CB_CUDA(G.ua.alloc(3 * N));
+  CB_CUDA(G.ub.alloc(3 * N));
+  CB_CUDA(G.vb.alloc(3 * N));
+  CB_CUDA(G.slot0.alloc(3 * (size_t)G.S));
+  CB_CUDA(G.slot1.alloc(3 * (size_t)G.S));
+  CB_CUDA(G.mass.alloc(N));
+  CB_CUDA(G.acc.alloc(3 * N));
+  CB_CUDA(G.contact.alloc(N));
+  CB_CUDA(G.sig_a.alloc(E * G.nq));
+  CB_CUDA(G.sig_b.alloc(E * G.nq));
+  CB_CUDA(G.epbar.alloc(E * G.nq));
+  CB_CUDA(G.work.alloc(4 * (size_t)G.C));
+  CB_CUDA(G.status.alloc(1));
+  CB_CUDA(G.step_ctr.alloc(1));
+  CB_CUDA(G.peak.alloc(G.insts.size()));
+  CB_CUDA(npe == 4 ? configure<4>((int)G.smem) : configure<10>((int)G.smem));
+  CB_CUDA(cudaStreamSynchronize(st));
+  return CI_OK;
+}
+
+int capture_graph(Group& G) {
+  if (G.graph) cudaGraphExecDestroy(G.graph);
+  G.graph = nullptr;
+  cudaGraph_t g = nullptr;
+  CB_CUDA(cudaStreamBeginCapture(G.stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t err = cudaSuccess;
+  for (int i = 0; i < kGraphSteps && err == cudaSuccess; i++) {
+    const FusedArgs F = group_args(G, i);
+    err = G.npe == 4 ? launch_batch<4>(G, F) : launch_batch<10>(G, F);
+  }
+  if (err == cudaSuccess) {
+    k_tick<<<1, 1, 0, G.stream>>>(G.step_ctr.p, kGraphSteps);
+    err = cudaGetLastError();
+  }
+  cudaError_t e2 = cudaStreamEndCapture(G.stream, &g);
+  if (err != cudaSuccess) return fail(CI_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(err));
+  if (e2 != cudaSuccess) return fail(CI_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e2));
+  err = cudaGraphInstantiate(&G.graph, g, 0);
+  cudaGraphDestroy(g);
+  if (err != cudaSuccess) return fail(CI_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(err));
+  return CI_OK;
+}
+
+// Reset to the initial state, lumped mass, a0 and half step; then enqueue all steps.
+int enqueue_run(Group& G) {
+  cudaStream_t st = G.stream;
+  const size_t N = G.N, E = G.E;
+  CB_CUDA(cudaMemsetAsync(G.ua.p, 0, sizeof(double) * 3 * N, st));
+  CB_CUDA(cudaMemcpyAsync(G.va.p, G.v0.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
+  CB_CUDA(cudaMemsetAsync(G.sig_a.p, 0, sizeof(float4) * E * G.nq, st));
+  CB_CUDA(cudaMemsetAsync(G.sig_b.p, 0, sizeof(float2) * E * G.nq, st));
+  CB_CUDA(cudaMemsetAsync(G.epbar.p, 0, sizeof(float) * E * G.nq, st));
+  CB_CUDA(cudaMemsetAsync(G.contact.p, 0, N, st));
+  CB_CUDA(cudaMemsetAsync(G.work.p, 0, sizeof(double) * 4 * G.C, st));
+  CB_CUDA(cudaMemsetAsync(G.status.p, 0, sizeof(unsigned int), st));
+  CB_CUDA(cudaMemsetAsync(G.step_ctr.p, 0, sizeof(int), st));
+  CB_CUDA(cudaMemsetAsync(G.peak.p, 0, sizeof(float) * G.insts.size(), st));
+  DevPlan P{};
+  P.chunks = G.chunks.p;
+  P.conn_local = G.conn.p;
+  P.color = G.color.p;
+  P.local_gid = G.lgid.p;
+  P.local_slot = G.lslot.p;
+  P.local_x0 = G.lx0.p;
+  P.slot_row = G.slot_row.p;
+  P.E = G.E;
+  P.N = G.N;
+  P.Lt = (int)G.Lt;
+  DevState D{};
+  for (int k = 0; k < 3; k++) {
+    D.u[k] = G.ua.p + k * N;
+    D.v[k] = G.va.p + k * N;
+    D.slot_f[k] = G.slot0.p + k * (size_t)G.S;
+  }
+  D.status = G.status.p;
+  D.chunk_work = G.work.p;
+  D.inst_ep = G.inst_ep.p;
+  const ElemParams p0{};
+  if (G.npe == 4)
+    k_elem<4, EM_MASS_HRZ, 256><<<G.C, 256, G.smem, st>>>(P, D, p0);
+  else
+    k_elem<10, EM_MASS_HRZ, 256><<<G.C, 256, G.smem, st>>>(P, D, p0);
+  CB_CUDA(cudaGetLastError());
+  k_mass_sum<<<(G.N + 255) / 256, 256, 0, st>>>(G.slot0.p, G.slot_row.p, G.mass.p, G.N);
+  CB_CUDA(cudaGetLastError());
+  NodeArrays A{};
+  for (int k = 0; k < 3; k++) {
+    A.u[k] = G.ua.p + k * N;
+    A.v[k] = G.va.p + k * N;
+    A.acc[k] = G.acc.p + k * N;
+  }
+  A.mass = G.mass.p;
+  A.d0 = G.d0.p;
+  A.contact = G.contact.p;
+  A.status = G.status.p;
+  NodeParams np0{};
+  np0.N = G.N;
+  k_node_init<true><<<(G.N + 255) / 256, 256, 0, st>>>(A, np0, G.inst_np.p, G.node_inst.p,
+                                                       G.d0f.p);
+  CB_CUDA(cudaGetLastError());
+  // all global steps: max_steps + 1 (the last instance's boundary finalisation)
+  const int total = G.max_steps + 1;
+  for (int done = 0; done < total; done += kGraphSteps) CB_CUDA(cudaGraphLaunch(G.graph, st));
+  return CI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ci_batch_create(const ci_instance* inst, int n, const ci_options* opt_in, ci_batch** out) {
+  if (!inst || n <= 0 || !out) return fail(CI_ERR_INVALID, "ci_batch_create: no instances");
+  *out = nullptr;
+  ci_options opt;
+  if (opt_in)
+    opt = *opt_in;
+  else
+    ci_default_options(&opt);
+  std::unique_ptr<ci_batch> b(new ci_batch());
+  b->device = opt.device;
+  CB_CUDA(cudaSetDevice(b->device));
+  b->inst.resize(n);
+  for (int i = 0; i < n; i++) {
+    const ci_instance& I = inst[i];
+    const int npe = I.mesh.nodes_per_element;
+    if (npe != 4 && npe != 10) return fail(CI_ERR_UNSUPPORTED, "instance with npe not 4 or 10");
+    if (!(I.dt > 0.0) || !(I.t_end >= 0.0)) return fail(CI_ERR_INVALID, "instance dt/t_end");
+    if (I.mat.beta != 0.0) return fail(CI_ERR_UNSUPPORTED, "only isotropic hardening (beta = 0)");
+    Inst& T = b->inst[i];
+    T.group = npe == 4 ? 0 : 1;
+    T.N = I.mesh.num_nodes;
+    T.E = I.mesh.num_elements;
+    T.npe = npe;
+    T.dt = I.dt;
+    long long ns = 0;
+    for (double t = 0.0; t <= I.t_end; t += I.dt) ns++;  // the reference's loop count
+    if (ns > (1 << 30)) return fail(CI_ERR_TOO_LARGE, "instance needs too many steps");
+    T.nsteps = (int)ns;
+    T.X.resize(3 * (size_t)T.N);
+    for (int k = 0; k < 3 * T.N; k++) T.X[k] = I.mesh.xloc[k] + I.pos[k % 3];
+    T.mat = I.mat;
+    T.wall = I.wall;
+    for (int k = 0; k < 3; k++) T.vel[k] = I.vel[k];
+  }
+  for (int gi = 0; gi < 2; gi++) {
+    std::unique_ptr<Group> G(new Group());
+    G->npe = gi == 0 ? 4 : 10;
+    G->nq = gi == 0 ? 1 : 4;
+    for (int i = 0; i < n; i++)
+      if (b->inst[i].group == gi) {
+        b->inst[i].index = (int)G->insts.size();
+        G->insts.push_back(i);
+      }
+    if (G->insts.empty()) continue;
+    G->block_threads = opt.block_threads ? opt.block_threads : 128;
+    G->elem_lanes = opt.elem_lanes ? opt.elem_lanes : 4;
+    G->chunk_nodes = opt.chunk_nodes ? opt.chunk_nodes : 2048;
+    CB_CUDA(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
+    int rc = build_group(b.get(), *G, inst, opt);
+    if (rc) return rc;
+    if ((rc = capture_graph(*G))) return rc;
+    b->g[gi] = std::move(G);
+  }
+  CB_CUDA(cudaEventCreate(&b->ev0));
+  CB_CUDA(cudaEventCreate(&b->ev1));
+  *out = b.release();
+  return CI_OK;
+}
+
+int ci_batch_run(ci_batch* b, float* device_ms) {
+  if (!b) return fail(CI_ERR_INVALID, "null batch");
+  CB_CUDA(cudaSetDevice(b->device));
+  // both groups start after ev0 and end before ev1 (device time of the whole batch)
+  cudaStream_t s0 = b->g[0] ? b->g[0]->stream : b->g[1]->stream;
+  CB_CUDA(cudaEventRecord(b->ev0, s0));
+  for (int gi = 0; gi < 2; gi++)
+    if (b->g[gi]) {
+      CB_CUDA(cudaStreamWaitEvent(b->g[gi]->stream, b->ev0, 0));
+      const int rc = enqueue_run(*b->g[gi]);
+      if (rc) return rc;
+    }
+  std::vector<cudaEvent_t> ends;
+  for (int gi = 0; gi < 2; gi++)
+    if (b->g[gi] && b->g[gi]->stream != s0) {
+      cudaEvent_t e;
+      CB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      CB_CUDA(cudaEventRecord(e, b->g[gi]->stream));
+      CB_CUDA(cudaStreamWaitEvent(s0, e, 0));
+      ends.push_back(e);
+    }
+  CB_CUDA(cudaEventRecord(b->ev1, s0));
+  CB_CUDA(cudaEventSynchronize(b->ev1));
+  for (cudaEvent_t e : ends) cudaEventDestroy(e);
+  CB_CUDA(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1));
+  if (device_ms) *device_ms = b->last_ms;
+  for (int gi = 0; gi < 2; gi++)
+    if (b->g[gi]) {
+      unsigned int st = 0;
+      CB_CUDA(cudaMemcpy(&st, b->g[gi]->status.p, sizeof(st), cudaMemcpyDeviceToHost));
+      if (st & ST_DEGENERATE) return fail(CI_ERR_DEGENERATE, "an element has det J <= 0");
+      if (st & ST_NONFINITE) return fail(CI_ERR_NONFINITE, "non-finite nodal state");
+    }
+  b->done = true;
+  return CI_OK;
+}
+
+int ci_batch_get_state(ci_batch* b, int i, double* x, double* v, float* epbar,
+                       unsigned char* contact, long long* nsteps) {
+  if (!b || i < 0 || i >= (int)b->inst.size()) return fail(CI_ERR_INVALID, "bad instance index");
+  if (!b->done) return fail(CI_ERR_INVALID, "ci_batch_run has not completed");
+  CB_CUDA(cudaSetDevice(b->device));
+  const Inst& T = b->inst[i];
+  const Group& G = *b->g[T.group];
+  const int N = T.N, E = T.E, nq = G.nq;
+  // final state in buffer A for an even step count, B for an odd one
+  const bool a = (T.nsteps & 1) == 0;
+  std::vector<double> hu(3 * (size_t)N), hv(3 * (size_t)N);
+  for (int k = 0; k < 3; k++) {
+    CB_CUDA(cudaMemcpy(&hu[(size_t)k * N], (a ? G.ua.p : G.ub.p) + (size_t)k * G.N + T.node_off,
+                       sizeof(double) * N, cudaMemcpyDeviceToHost));
+    CB_CUDA(cudaMemcpy(&hv[(size_t)k * N], (a ? G.va.p : G.vb.p) + (size_t)k * G.N + T.node_off,
+                       sizeof(double) * N, cudaMemcpyDeviceToHost));
+  }
+  std::vector<unsigned char> hc(N);
+  CB_CUDA(cudaMemcpy(hc.data(), G.contact.p + T.node_off, N, cudaMemcpyDeviceToHost));
+  std::vector<float> hep((size_t)E * nq);
+  CB_CUDA(cudaMemcpy(hep.data(), G.epbar.p + (size_t)T.elem_off * nq, sizeof(float) * hep.size(),
+                     cudaMemcpyDeviceToHost));
+  for (int p = 0; p < N; p++) {
+    const int o = T.node_orig[p];
+    for (int k = 0; k < 3; k++) {
+      if (x) x[3 * (size_t)o + k] = T.X[3 * (size_t)o + k] + hu[(size_t)k * N + p];
+      if (v) v[3 * (size_t)o + k] = hv[(size_t)k * N + p];
+    }
+    if (contact) contact[o] = hc[p];
+  }
+  if (epbar)
+    for (int pe = 0; pe < E; pe++)
+      for (int q = 0; q < nq; q++)
+        epbar[(size_t)T.elem_orig[pe] * nq + q] = hep[(size_t)pe * nq + q];
+  if (nsteps) *nsteps = T.nsteps;
+  return CI_OK;
+}
+
+int ci_batch_destroy(ci_batch* b) {
+  if (!b) return CI_OK;
+  cudaSetDevice(b->device);
+  for (int gi = 0; gi < 2; gi++)
+    if (b->g[gi]) cudaStreamSynchronize(b->g[gi]->stream);
+  delete b;
+  return CI_OK;
+}
+
+}  // extern "C"

@@ -36,17 +36,6 @@ struct DevPlan {
   int E, N, Lt;
 };
 
-struct DevState {
-  double* u[3];        // displacement from the reference positions, SoA [N]
-  double* v[3];        // half-step velocity, SoA [N]
-  float* slot_f[3];    // partial node forces per slot, SoA [S]
-  float4* sig_a;       // [nq][E] stress xx yy zz xy
-  float2* sig_b;       // [nq][E] stress yz xz
-  float* epbar;        // [nq][E] equivalent plastic strain
-  double* chunk_work;  // [C][4] internal work, plastic work, volume, unused (running sums)
-  unsigned int* status;
-};
-
 struct ElemParams {
   float dt;
   float lambda, mu;       // Lame constants
@@ -55,11 +44,26 @@ struct ElemParams {
   int accum_energy;       // accumulate work terms into chunk_work
 };
 
+struct DevState {
+  double* u[3];        // displacement from the reference positions, SoA [N]
+  double* v[3];        // half-step velocity, SoA [N]
+  float* slot_f[3];    // partial node forces per slot, SoA [S]
+  float4* sig_a;       // [E][nq] stress xx yy zz xy
+  float2* sig_b;       // [E][nq] stress yz xz
+  float* epbar;        // [E][nq] equivalent plastic strain
+  double* chunk_work;  // [C][4] internal work, plastic work, volume, unused (running sums)
+  unsigned int* status;
+  const ElemParams* inst_ep;  // per-instance parameters of a batched solve (else null)
+};
+
+
 struct NodeParams {
   double dt;
   double g[3];
   double wall_n[3];
   double wall_k;
+  float gf[3];  // g and wall normal rounded to FP32
+  float nf[3];
   int N;
 };
 
@@ -248,7 +252,7 @@ __device__ __forceinline__ void element_force(const ElemParams& p, const DevStat
         wint = fmaf(0.5f * wd, w, wint);
       }
     } else {
-      const size_t qi = (size_t)q * E + e;
+      const size_t qi = (size_t)e * R::NQ + q;
       const float4 sa = S.sig_a[qi];
       const float2 sb = S.sig_b[qi];
       float ep = S.epbar[qi];
@@ -312,9 +316,10 @@ __device__ __forceinline__ float block_sum(float v, float* red) {
 
 // K1 / K3.  Shared memory: x[3][Lmax] du[3][Lmax] acc[3][Lmax] floats + reduction.
 template <int NPE, int MODE, int BS>
-__global__ void __launch_bounds__(BS) k_elem(DevPlan P, DevState S, ElemParams p) {
+__global__ void __launch_bounds__(BS) k_elem(DevPlan P, DevState S, ElemParams p_arg) {
   extern __shared__ float sm[];
   const ChunkInfo ch = P.chunks[blockIdx.x];
+  const ElemParams p = S.inst_ep ? S.inst_ep[ch.inst] : p_arg;
   const int L = ch.n_local;
   float* sx = sm;
   float* sd = sm + 3 * L;
@@ -467,6 +472,7 @@ struct FusedArgs {
   float* halo_cur[3];
   const float* mass;
   const double* d0;
+  const float* d0f;  // d0 rounded to FP32 (wall screening)
   unsigned char* contact;
   float* acc[3];
   float4* sig_a;
@@ -476,46 +482,102 @@ struct FusedArgs {
   unsigned int* status;
   int bnd_final;  // boundary nodes already hold S^n in the cur buffer
   int store_acc;
+  // batched solves (k_step<..., BATCH = true>): per-instance parameters and step counts;
+  // the global step is *step_ctr + step_off.  An instance steps while step < nsteps,
+  // finalises its boundary nodes at step == nsteps and idles afterwards.
+  const ElemParams* inst_ep;
+  const NodeParams* inst_np;
+  const int* inst_nsteps;
+  const int* step_ctr;
+  int step_off;
 };
 
+// Per-chunk view of the step: parameters, whether to step, finalise only, or idle.
+struct ChunkStep {
+  ElemParams ep;
+  NodeParams np;
+  int bnd_final;
+  int mode;  // 0 step, 1 finalise boundary nodes only, 2 idle
+};
+
+template <bool BATCH>
+__device__ __forceinline__ ChunkStep chunk_step(const FusedArgs& A, const ChunkInfo& ch,
+                                                const ElemParams& ep, const NodeParams& np) {
+  ChunkStep c;
+  if (!BATCH) {
+    c.ep = ep;
+    c.np = np;
+    c.bnd_final = A.bnd_final;
+    c.mode = 0;
+    return c;
+  }
+  const int k = *A.step_ctr + A.step_off;
+  const int n = A.inst_nsteps[ch.inst];
+  c.ep = A.inst_ep[ch.inst];
+  c.np = A.inst_np[ch.inst];
+  c.bnd_final = k == 0;
+  c.mode = k < n ? 0 : (k == n ? 1 : 2);
+  return c;
+}
+
 // One node's central-difference update from its total internal force f.
-// u, v: in S^n, out S^{n+1}.  Rounding is explicit (no contraction freedom).
+// u, v: in S^n, out S^{n+1}; a: the acceleration applied.  Rounding is explicit (no
+// contraction freedom), so every chunk that updates the same boundary node gets the
+// same bits.  FP64 work is 6 FMAs per node: u + dt v and v + dt a.  The acceleration
+// -f/m + g is formed in FP32 (as accurate as f); the wall distance is screened in FP32
+// with a margin above its worst rounding error and only evaluated in FP64 near or
+// inside the wall.
 __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float fy, float fz, float m,
-                                          double d0, double (&u)[3], double (&v)[3],
-                                          double (&a)[3], bool& in_contact) {
+                                          float d0f, const double* d0, int g, double (&u)[3],
+                                          double (&v)[3], float (&a)[3], bool& in_contact) {
   const float rm = __frcp_rn(m);
-  a[0] = __dadd_rn((double)__fmul_rn(-fx, rm), p.g[0]);
-  a[1] = __dadd_rn((double)__fmul_rn(-fy, rm), p.g[1]);
-  a[2] = __dadd_rn((double)__fmul_rn(-fz, rm), p.g[2]);
+  a[0] = __fadd_rn(__fmul_rn(-fx, rm), p.gf[0]);
+  a[1] = __fadd_rn(__fmul_rn(-fy, rm), p.gf[1]);
+  a[2] = __fadd_rn(__fmul_rn(-fz, rm), p.gf[2]);
   double un[3];
+  float uf[3];
 #pragma unroll
-  for (int k = 0; k < 3; k++) un[k] = __fma_rn(p.dt, v[k], u[k]);
-  const double d = __fma_rn(p.wall_n[2], un[2], __fma_rn(p.wall_n[1], un[1],
-                            __fma_rn(p.wall_n[0], un[0], d0)));
-  in_contact = d < 0.0;
-  if (in_contact) {
-    const double c = __ddiv_rn(__dmul_rn(-d, p.wall_k), (double)m);
+  for (int k = 0; k < 3; k++) {
+    un[k] = __fma_rn(p.dt, v[k], u[k]);
+    uf[k] = (float)un[k];
+  }
+  // |d32 - d| <= 2^-22 (|d0| + |u|_1) for |n_k| <= 1; 1e-6 (1 + ...) covers it
+  const float d32 = __fadd_rn(d0f, __fadd_rn(__fmul_rn(p.nf[0], uf[0]),
+                                  __fadd_rn(__fmul_rn(p.nf[1], uf[1]), __fmul_rn(p.nf[2], uf[2]))));
+  const float margin = 1e-6f * (1.f + fabsf(d0f) + fabsf(uf[0]) + fabsf(uf[1]) + fabsf(uf[2]));
+  in_contact = false;
+  double ad[3] = {(double)a[0], (double)a[1], (double)a[2]};
+  if (!(d32 > margin)) {
+    const double d = __fma_rn(p.wall_n[2], un[2], __fma_rn(p.wall_n[1], un[1],
+                              __fma_rn(p.wall_n[0], un[0], d0[g])));
+    if (d < 0.0) {
+      in_contact = true;
+      const double c = __ddiv_rn(__dmul_rn(-d, p.wall_k), (double)m);
 #pragma unroll
-    for (int k = 0; k < 3; k++) a[k] = __fma_rn(c, p.wall_n[k], a[k]);
+      for (int k = 0; k < 3; k++) {
+        ad[k] = __fma_rn(c, p.wall_n[k], ad[k]);
+        a[k] = (float)ad[k];
+      }
+    }
   }
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    v[k] = __fma_rn(p.dt, a[k], v[k]);
+    v[k] = __fma_rn(p.dt, ad[k], v[k]);
     u[k] = un[k];
   }
 }
 
 __device__ __forceinline__ void store_node(const FusedArgs& A, double* const (&uo)[3],
                                            double* const (&vo)[3], int g, const double (&u)[3],
-                                           const double (&v)[3], const double (&a)[3],
+                                           const double (&v)[3], const float (&a)[3],
                                            bool in_contact, bool store_acc) {
   bool finite = true;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     uo[k][g] = u[k];
     vo[k][g] = v[k];
-    finite = finite && isfinite(v[k]);
-    if (store_acc) A.acc[k][g] = (float)a[k];
+    finite = finite && isfinite((float)v[k]);
+    if (store_acc) A.acc[k][g] = a[k];
   }
   if (!finite) atomicOr(A.status, (unsigned)ST_NONFINITE);
   const unsigned char old = A.contact[g];
@@ -523,20 +585,16 @@ __device__ __forceinline__ void store_node(const FusedArgs& A, double* const (&u
   if (flag != old) A.contact[g] = flag;
 }
 
-template <int NPE, int MODE, int BS>
-__global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep, NodeParams np) {
-  extern __shared__ float sm[];
+// Stage S^n of every local node of the chunk in shared memory (x relative to the
+// chunk origin, dt v), bringing boundary nodes from S^{n-1} to S^n first.
+template <int BS>
+__device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams& ep,
+                                            const NodeParams& np, const ChunkInfo& ch,
+                                            int bnd_final, float* sx, float* sd, float* sa) {
   const DevPlan& P = A.P;
-  const ChunkInfo ch = P.chunks[blockIdx.x];
   const int L = ch.n_local;
-  float* sx = sm;
-  float* sd = sm + 3 * L;
-  float* sa = sm + 6 * L;
-  __shared__ float red[BS / 32];
-
-  // -- stage S^n of every local node (finalising boundary nodes) ----------------------
   // interior nodes: contiguous owned range, independent loads (unrolled for MLP)
-  const int n_direct = A.bnd_final ? L : ch.n_int;
+  const int n_direct = bnd_final ? L : ch.n_int;
 #pragma unroll 4
   for (int l = threadIdx.x; l < n_direct; l += BS) {
     const int lb = ch.local_begin + l;
@@ -568,9 +626,9 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep, NodePar
       u[k] = A.u_prv[k][g];
       v[k] = A.v_prv[k][g];
     }
-    double a[3];
+    float a[3];
     bool hit;
-    node_step(np, fx, fy, fz, A.mass[g], A.d0[g], u, v, a, hit);
+    node_step(np, fx, fy, fz, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit);
     if (l < ch.n_own) store_node(A, A.u_cur, A.v_cur, g, u, v, a, hit, false);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -579,9 +637,68 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep, NodePar
       sa[k * L + l] = 0.f;
     }
   }
+}
+
+// Interior nodes S^n -> S^{n+1} (other buffer); boundary partial forces to the halo.
+template <int BS>
+__device__ __forceinline__ void node_epilogue(const FusedArgs& A, const NodeParams& np,
+                                              const ChunkInfo& ch, const float* sa) {
+  const DevPlan& P = A.P;
+  const int L = ch.n_local;
+#pragma unroll 2
+  for (int l = threadIdx.x; l < L; l += BS) {
+    if (l < ch.n_int) {
+      const int g = ch.own_begin + l;
+      double u[3], v[3];
+      float a[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        u[k] = A.u_cur[k][g];
+        v[k] = A.v_cur[k][g];
+      }
+      bool hit;
+      node_step(np, sa[l], sa[L + l], sa[2 * L + l], A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit);
+      store_node(A, A.u_prv, A.v_prv, g, u, v, a, hit, A.store_acc != 0);
+    } else {
+      const int s = P.local_slot[ch.local_begin + l];
+      A.halo_cur[0][s] = sa[l];
+      A.halo_cur[1][s] = sa[L + l];
+      A.halo_cur[2][s] = sa[2 * L + l];
+    }
+  }
+}
+
+template <int BS>
+__device__ __forceinline__ void add_chunk_work(const FusedArgs& A, float wint, float wp, float* red) {
+  const float t0 = block_sum<BS>(wint, red);
+  const float t1 = block_sum<BS>(wp, red);
+  if (threadIdx.x == 0) {
+    double* cw = A.chunk_work + 4 * (size_t)blockIdx.x;
+    cw[0] += (double)t0;
+    cw[1] += (double)t1;
+  }
+}
+
+// Fused step, one thread per element (tet4, and the tet10 reference variant).
+template <int NPE, int MODE, int BS, bool BATCH = false>
+__global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
+  extern __shared__ float sm[];
+  const DevPlan& P = A.P;
+  const ChunkInfo ch = P.chunks[blockIdx.x];
+  const ChunkStep cs = chunk_step<BATCH>(A, ch, ep_arg, np_arg);
+  if (cs.mode == 2) return;
+  const ElemParams& ep = cs.ep;
+  const NodeParams& np = cs.np;
+  const int L = ch.n_local;
+  float* sx = sm;
+  float* sd = sm + 3 * L;
+  float* sa = sm + 6 * L;
+  __shared__ float red[BS / 32];
+
+  stage_nodes<BS>(A, ep, np, ch, cs.bnd_final, sx, sd, sa);
+  if (cs.mode == 1) return;
   __syncthreads();
 
-  // -- elements, colour-ordered accumulation (as k_elem) ------------------------------
   DevState S;
   S.sig_a = A.sig_a;
   S.sig_b = A.sig_b;
@@ -624,42 +741,243 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep, NodePar
     }
   }
   __syncthreads();
+  node_epilogue<BS>(A, np, ch, sa);
+  if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
+}
 
-  // -- epilogue: interior nodes S^n -> S^{n+1}; boundary partials to the halo ---------
-#pragma unroll 2
-  for (int l = threadIdx.x; l < L; l += BS) {
-    if (l < ch.n_int) {
-      const int g = ch.own_begin + l;
-      double u[3], v[3], a[3];
+// ---------------------------------------------------------------------------
+// tet10 with one lane per Gauss point (lanes 4k..4k+3 of a warp share an element).
+//
+// With barycentrics L = (xi, eta, 1-xi-eta-zeta, zeta) at the lane's point and
+// A_c = 4 L_c, the shape-function gradients are G_0 = (A0-1, 0, 0), G_1 = (0, A1-1, 0),
+// G_2 = -(A2-1)(1,1,1), G_3 = (0, 0, A3-1), G_4 = (A1, A0, 0),
+// G_5 = (-A1, A2-A1, -A1), G_6 = (A2-A0, -A0, -A0), G_7 = (A3, 0, A0),
+// G_8 = (0, A3, A1), G_9 = (-A3, -A3, A2-A3).  J = sum_i x_i G_i^T and grad du are
+// built from nodes streamed out of shared memory; the lane's Gauss-point force
+// contributions P G_i are summed over the four lanes by an xor butterfly (fixed
+// order, so the result is bitwise reproducible).
+// ---------------------------------------------------------------------------
+struct Tet10QP {
+  float A0, A1, A2, A3;
+};
+
+__device__ __forceinline__ Tet10QP tet10_qp(int q) {
+  const float a = 0.58541019662496845f, b = 0.13819660112501052f;
+  Tet10QP t;
+  t.A0 = 4.f * (q == 1 ? a : b);
+  t.A1 = 4.f * (q == 2 ? a : b);
+  t.A2 = 4.f * (q == 0 ? a : b);
+  t.A3 = 4.f * (q == 3 ? a : b);
+  return t;
+}
+
+// c[j] += x * G_i[j] for node i of the tet10 at this lane's point.
+template <int I>
+__device__ __forceinline__ void tet10_grad_acc(const Tet10QP& t, float x, float (&c)[3]) {
+  if (I == 0) c[0] = fmaf(t.A0 - 1.f, x, c[0]);
+  if (I == 1) c[1] = fmaf(t.A1 - 1.f, x, c[1]);
+  if (I == 2) {
+    const float g = (1.f - t.A2) * x;
+    c[0] += g; c[1] += g; c[2] += g;
+  }
+  if (I == 3) c[2] = fmaf(t.A3 - 1.f, x, c[2]);
+  if (I == 4) { c[0] = fmaf(t.A1, x, c[0]); c[1] = fmaf(t.A0, x, c[1]); }
+  if (I == 5) { c[0] = fmaf(-t.A1, x, c[0]); c[1] = fmaf(t.A2 - t.A1, x, c[1]); c[2] = fmaf(-t.A1, x, c[2]); }
+  if (I == 6) { c[0] = fmaf(t.A2 - t.A0, x, c[0]); c[1] = fmaf(-t.A0, x, c[1]); c[2] = fmaf(-t.A0, x, c[2]); }
+  if (I == 7) { c[0] = fmaf(t.A3, x, c[0]); c[2] = fmaf(t.A0, x, c[2]); }
+  if (I == 8) { c[1] = fmaf(t.A3, x, c[1]); c[2] = fmaf(t.A1, x, c[2]); }
+  if (I == 9) { c[0] = fmaf(-t.A3, x, c[0]); c[1] = fmaf(-t.A3, x, c[1]); c[2] = fmaf(t.A2 - t.A3, x, c[2]); }
+}
+
+// f = P G_i (row a of P times the gradient of node i)
+template <int I>
+__device__ __forceinline__ float tet10_force(const Tet10QP& t, const float* Pa) {
+  if (I == 0) return (t.A0 - 1.f) * Pa[0];
+  if (I == 1) return (t.A1 - 1.f) * Pa[1];
+  if (I == 2) return (1.f - t.A2) * (Pa[0] + Pa[1] + Pa[2]);
+  if (I == 3) return (t.A3 - 1.f) * Pa[2];
+  if (I == 4) return fmaf(t.A1, Pa[0], t.A0 * Pa[1]);
+  if (I == 5) return fmaf(-t.A1, Pa[0], fmaf(t.A2 - t.A1, Pa[1], -t.A1 * Pa[2]));
+  if (I == 6) return fmaf(t.A2 - t.A0, Pa[0], -t.A0 * (Pa[1] + Pa[2]));
+  if (I == 7) return fmaf(t.A3, Pa[0], t.A0 * Pa[2]);
+  if (I == 8) return fmaf(t.A3, Pa[1], t.A1 * Pa[2]);
+  return fmaf(-t.A3, Pa[0] + Pa[1], (t.A2 - t.A3) * Pa[2]);
+}
+
+template <int I>
+__device__ __forceinline__ void tet10_gather(const Tet10QP& t, const float* sx, const float* sd,
+                                             int L, int l, float (&J)[9], float (&Gu)[9]) {
+  float cj[3], cu[3];
 #pragma unroll
-      for (int k = 0; k < 3; k++) {
-        u[k] = A.u_cur[k][g];
-        v[k] = A.v_cur[k][g];
+  for (int a = 0; a < 3; a++) {
+    cj[0] = J[3 * a]; cj[1] = J[3 * a + 1]; cj[2] = J[3 * a + 2];
+    tet10_grad_acc<I>(t, sx[a * L + l], cj);
+    J[3 * a] = cj[0]; J[3 * a + 1] = cj[1]; J[3 * a + 2] = cj[2];
+    cu[0] = Gu[3 * a]; cu[1] = Gu[3 * a + 1]; cu[2] = Gu[3 * a + 2];
+    tet10_grad_acc<I>(t, sd[a * L + l], cu);
+    Gu[3 * a] = cu[0]; Gu[3 * a + 1] = cu[1]; Gu[3 * a + 2] = cu[2];
+  }
+}
+
+template <int I>
+__device__ __forceinline__ void tet10_node_force(const Tet10QP& t, const float (&Pm)[9], int q,
+                                                 float (&keep)[3][3]) {
+  float f[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    float v = tet10_force<I>(t, &Pm[3 * a]);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    f[a] = v;
+  }
+  if ((I & 3) == q) {
+#pragma unroll
+    for (int a = 0; a < 3; a++) keep[I >> 2][a] = f[a];
+  }
+}
+
+template <int MODE, int BS, bool BATCH = false>
+__global__ void __launch_bounds__(BS) k_step_qp10(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
+  extern __shared__ float sm[];
+  const DevPlan& P = A.P;
+  const ChunkInfo ch = P.chunks[blockIdx.x];
+  const ChunkStep cs = chunk_step<BATCH>(A, ch, ep_arg, np_arg);
+  if (cs.mode == 2) return;
+  const ElemParams& ep = cs.ep;
+  const NodeParams& np = cs.np;
+  const int L = ch.n_local;
+  float* sx = sm;
+  float* sd = sm + 3 * L;
+  float* sa = sm + 6 * L;
+  __shared__ float red[BS / 32];
+
+  stage_nodes<BS>(A, ep, np, ch, cs.bnd_final, sx, sd, sa);
+  if (cs.mode == 1) return;
+  __syncthreads();
+
+  const int q = threadIdx.x & 3;
+  const Tet10QP t = tet10_qp(q);
+  constexpr float W = 1.0f / 24.0f;
+  const int E = P.E;
+  float wint = 0.f, wp = 0.f;
+  constexpr int EPW = BS / 4;  // elements per window
+  for (int w = ch.elem_begin; w < ch.elem_end; w += EPW) {
+    const int e = w + (threadIdx.x >> 2);
+    const bool act = e < ch.elem_end;
+    const int ee = act ? e : ch.elem_begin;  // inactive lanes shadow a valid element
+    int ln[10];
+#pragma unroll
+    for (int a = 0; a < 10; a++) ln[a] = P.conn_local[(size_t)a * E + ee];
+    const size_t qi = (size_t)ee * 4 + q;
+    float4 s4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 s2 = make_float2(0.f, 0.f);
+    float ep0 = 0.f;
+    if (MODE == EM_J2) {
+      s4 = A.sig_a[qi];
+      s2 = A.sig_b[qi];
+      ep0 = A.epbar[qi];
+    }
+    float J[9], Gu[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) J[k] = Gu[k] = 0.f;
+    tet10_gather<0>(t, sx, sd, L, ln[0], J, Gu);
+    tet10_gather<1>(t, sx, sd, L, ln[1], J, Gu);
+    tet10_gather<2>(t, sx, sd, L, ln[2], J, Gu);
+    tet10_gather<3>(t, sx, sd, L, ln[3], J, Gu);
+    tet10_gather<4>(t, sx, sd, L, ln[4], J, Gu);
+    tet10_gather<5>(t, sx, sd, L, ln[5], J, Gu);
+    tet10_gather<6>(t, sx, sd, L, ln[6], J, Gu);
+    tet10_gather<7>(t, sx, sd, L, ln[7], J, Gu);
+    tet10_gather<8>(t, sx, sd, L, ln[8], J, Gu);
+    tet10_gather<9>(t, sx, sd, L, ln[9], J, Gu);
+    float Ji[9];
+    const float detJ = inv3f(J, Ji);
+    if (act && !(detJ > 0.f)) atomicOr(A.status, (unsigned)ST_DEGENERATE);
+    const float wd = act ? W * detJ : 0.f;
+    float Lg[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++)
+        Lg[3 * a + b] = Gu[3 * a + 0] * Ji[0 * 3 + b] + Gu[3 * a + 1] * Ji[1 * 3 + b] +
+                        Gu[3 * a + 2] * Ji[2 * 3 + b];
+    const float de[6] = {Lg[0], Lg[4], Lg[8], Lg[1] + Lg[3], Lg[5] + Lg[7], Lg[2] + Lg[6]};
+    const float tr = de[0] + de[1] + de[2];
+    const float s0[6] = {s4.x, s4.y, s4.z, s4.w, s2.x, s2.y};
+    float s[6];
+    s[0] = s0[0] + ep.lambda * tr + 2.f * ep.mu * de[0];
+    s[1] = s0[1] + ep.lambda * tr + 2.f * ep.mu * de[1];
+    s[2] = s0[2] + ep.lambda * tr + 2.f * ep.mu * de[2];
+    s[3] = s0[3] + ep.mu * de[3];
+    s[4] = s0[4] + ep.mu * de[4];
+    s[5] = s0[5] + ep.mu * de[5];
+    float epn = ep0;
+    if (MODE == EM_J2) {
+      j2_return(ep, s, epn);
+      if (act) {
+        A.sig_a[qi] = make_float4(s[0], s[1], s[2], s[3]);
+        A.sig_b[qi] = make_float2(s[4], s[5]);
+        A.epbar[qi] = epn;
       }
-      bool hit;
-      node_step(np, sa[l], sa[L + l], sa[2 * L + l], A.mass[g], A.d0[g], u, v, a, hit);
-      store_node(A, A.u_prv, A.v_prv, g, u, v, a, hit, A.store_acc != 0);
-    } else {
-      const int s = P.local_slot[ch.local_begin + l];
-      A.halo_cur[0][s] = sa[l];
-      A.halo_cur[1][s] = sa[L + l];
-      A.halo_cur[2][s] = sa[2 * L + l];
+    }
+    if (ep.accum_energy && act) {
+      float wq = 0.f;
+#pragma unroll
+      for (int k = 0; k < 6; k++) wq = fmaf(s0[k] + s[k], de[k], wq);
+      wint = fmaf(0.5f * wd, wq, wint);
+      if (MODE == EM_J2) wp = fmaf(wd * (ep.sy0 + ep.H * epn), epn - ep0, wp);
+    }
+    const float Sg[9] = {s[0], s[3], s[5], s[3], s[1], s[4], s[5], s[4], s[2]};
+    float Pm[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        Pm[3 * a + j] = wd * (Sg[3 * a + 0] * Ji[3 * j + 0] + Sg[3 * a + 1] * Ji[3 * j + 1] +
+                              Sg[3 * a + 2] * Ji[3 * j + 2]);
+    float keep[3][3];
+    tet10_node_force<0>(t, Pm, q, keep);
+    tet10_node_force<1>(t, Pm, q, keep);
+    tet10_node_force<2>(t, Pm, q, keep);
+    tet10_node_force<3>(t, Pm, q, keep);
+    tet10_node_force<4>(t, Pm, q, keep);
+    tet10_node_force<5>(t, Pm, q, keep);
+    tet10_node_force<6>(t, Pm, q, keep);
+    tet10_node_force<7>(t, Pm, q, keep);
+    tet10_node_force<8>(t, Pm, q, keep);
+    tet10_node_force<9>(t, Pm, q, keep);
+    // lane q owns nodes q, q+4 and (for q < 2) q+8
+    const int own0 = q == 0 ? ln[0] : q == 1 ? ln[1] : q == 2 ? ln[2] : ln[3];
+    const int own1 = q == 0 ? ln[4] : q == 1 ? ln[5] : q == 2 ? ln[6] : ln[7];
+    const int own2 = q == 0 ? ln[8] : ln[9];
+    const int col = act ? P.color[e] : -1;
+    const int c0 = P.color[w];
+    const int c1 = P.color[min(w + EPW, ch.elem_end) - 1];
+    for (int k = c0; k <= c1; k++) {
+      __syncthreads();
+      if (col == k) {
+        sa[own0] += keep[0][0];
+        sa[L + own0] += keep[0][1];
+        sa[2 * L + own0] += keep[0][2];
+        sa[own1] += keep[1][0];
+        sa[L + own1] += keep[1][1];
+        sa[2 * L + own1] += keep[1][2];
+        if (q < 2) {
+          sa[own2] += keep[2][0];
+          sa[L + own2] += keep[2][1];
+          sa[2 * L + own2] += keep[2][2];
+        }
+      }
     }
   }
-  if (ep.accum_energy) {
-    const float t0 = block_sum<BS>(wint, red);
-    const float t1 = block_sum<BS>(wp, red);
-    if (threadIdx.x == 0) {
-      double* cw = A.chunk_work + 4 * (size_t)blockIdx.x;
-      cw[0] += (double)t0;
-      cw[1] += (double)t1;
-    }
-  }
+  __syncthreads();
+  node_epilogue<BS>(A, np, ch, sa);
+  if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
 }
 
 // S^N of the boundary nodes after the last fused step of a call: reads S^{N-1} from
 // the prv buffer and the halo of step N-1, writes S^N (and a^N) to the cur buffer.
-__global__ void __launch_bounds__(256) k_finalize_boundary(FusedArgs A, NodeParams np,
+static __global__ void __launch_bounds__(256) k_finalize_boundary(FusedArgs A, NodeParams np,
                                                            const int* bnd_nodes, int nb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nb) return;
@@ -671,19 +989,78 @@ __global__ void __launch_bounds__(256) k_finalize_boundary(FusedArgs A, NodePara
     fy = __fadd_rn(fy, A.halo_prv[1][s]);
     fz = __fadd_rn(fz, A.halo_prv[2][s]);
   }
-  double u[3], v[3], a[3];
+  double u[3], v[3];
+  float a[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     u[k] = A.u_prv[k][g];
     v[k] = A.v_prv[k][g];
   }
   bool hit;
-  node_step(np, fx, fy, fz, A.mass[g], A.d0[g], u, v, a, hit);
+  node_step(np, fx, fy, fz, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit);
   store_node(A, A.u_cur, A.v_cur, g, u, v, a, hit, true);
 }
 
+// a0 from zero internal force (wall at the start positions, gravity) and the half step
+// v += dt/2 a0 (include/dynamics.h:454-463), rounded like node_step.
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_node_init(NodeArrays A, NodeParams p_arg,
+                                                   const NodeParams* inst_np, const int* node_inst,
+                                                   const float* d0f) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= p_arg.N) return;
+  const NodeParams p = BATCH ? inst_np[node_inst[n]] : p_arg;
+  double u[3], v[3], ad[3];
+  float uf[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    u[k] = A.u[k][n];
+    v[k] = A.v[k][n];
+    uf[k] = (float)u[k];
+    ad[k] = (double)p.gf[k];
+  }
+  const float d32 = __fadd_rn(d0f[n], __fadd_rn(__fmul_rn(p.nf[0], uf[0]),
+                                  __fadd_rn(__fmul_rn(p.nf[1], uf[1]), __fmul_rn(p.nf[2], uf[2]))));
+  const float margin = 1e-6f * (1.f + fabsf(d0f[n]) + fabsf(uf[0]) + fabsf(uf[1]) + fabsf(uf[2]));
+  unsigned char flag = 0;
+  if (!(d32 > margin)) {
+    const double d = __fma_rn(p.wall_n[2], u[2], __fma_rn(p.wall_n[1], u[1],
+                              __fma_rn(p.wall_n[0], u[0], A.d0[n])));
+    if (d < 0.0) {
+      flag = 3;
+      const double c = __ddiv_rn(__dmul_rn(-d, p.wall_k), (double)A.mass[n]);
+#pragma unroll
+      for (int k = 0; k < 3; k++) ad[k] = __fma_rn(c, p.wall_n[k], ad[k]);
+    }
+  }
+  bool finite = true;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double vn = __fma_rn(0.5 * p.dt, ad[k], v[k]);
+    finite = finite && isfinite((float)vn);
+    A.v[k][n] = vn;
+    A.acc[k][n] = (float)ad[k];
+  }
+  A.contact[n] = flag;
+  if (!finite) atomicOr(A.status, (unsigned)ST_NONFINITE);
+}
+
+// Adds n to the batched step counter (after each captured block of steps).
+static __global__ void k_tick(int* step_ctr, int n) { *step_ctr += n; }
+
+// Peak |u| over a node range since the last reset (one FP32 max per block, fixed order).
+static __global__ void k_peak_disp(const double* ux, const double* uy, const double* uz,
+                                   const int* node_inst, float* inst_peak, int N) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const float m = (float)sqrt(ux[n] * ux[n] + uy[n] * uy[n] + uz[n] * uz[n]);
+  // non-negative floats order like their bit patterns: integer max is exact and
+  // order-independent
+  atomicMax(reinterpret_cast<int*>(inst_peak) + node_inst[n], __float_as_int(m));
+}
+
 // Lumped mass: sum of the node's slots (component 0) in chunk order.
-__global__ void k_mass_sum(const float* slot_m, const int* slot_row, float* mass, int N) {
+static __global__ void k_mass_sum(const float* slot_m, const int* slot_row, float* mass, int N) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
   float m = 0.f;
@@ -692,7 +1069,7 @@ __global__ void k_mass_sum(const float* slot_m, const int* slot_row, float* mass
 }
 
 // Assembled internal force of a one-shot call: slot sums to FP64 [3][N].
-__global__ void k_force_sum(const float* sx, const float* sy, const float* sz, const int* slot_row,
+static __global__ void k_force_sum(const float* sx, const float* sy, const float* sz, const int* slot_row,
                             double* f, int N) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
@@ -709,7 +1086,7 @@ __global__ void k_force_sum(const float* sx, const float* sy, const float* sz, c
 
 // Energy terms at the current state, one FP64 partial per block (fixed-order sums):
 // out[blk][0] kinetic (v_n = v - dt/2 a), [1] contact potential, [2] gravity work.
-__global__ void k_energy(NodeArrays A, NodeParams p, double* out) {
+static __global__ void k_energy(NodeArrays A, NodeParams p, double* out) {
   __shared__ double red[3][256];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   double ke = 0.0, phi = 0.0, wg = 0.0;

@@ -32,7 +32,7 @@ struct ChunkInfo {
   int n_local;      // owned + ghost
   int local_begin;  // offset of this chunk's entries in the local tables
   int n_int;        // interior nodes (touched by this chunk only) are local ids [0, n_int)
-  int pad;
+  int inst;         // instance of a batched solve (0 for a single mesh)
 };
 
 struct Plan {

@@ -60,6 +60,15 @@ struct DBuf {
 
 }  // namespace
 
+namespace ci {
+// Sets the message returned by ci_last_error on this thread (used by other files of
+// the library) and passes the status code through.
+int set_last_error(int code, const char* msg) {
+  g_last_error = msg;
+  return code;
+}
+}  // namespace ci
+
 struct ci_solver {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -94,6 +103,7 @@ struct ci_solver {
   DBuf<float> d_slot;      // [3][S]
   DBuf<float> d_mass;      // [N]
   DBuf<double> d_d0;       // [N]
+  DBuf<float> d_d0f;       // [N]
   DBuf<unsigned char> d_contact;
   DBuf<float> d_acc;       // [3][N]
   DBuf<float4> d_sig_a;
@@ -137,6 +147,7 @@ struct ci_solver {
     D.epbar = d_epbar.p;
     D.chunk_work = d_work.p;
     D.status = d_status.p;
+    D.inst_ep = nullptr;
     return D;
   }
   ci::ElemParams elem_params(float dtf, bool energy) const {
@@ -185,6 +196,7 @@ struct ci_solver {
     }
     F.mass = d_mass.p;
     F.d0 = d_d0.p;
+    F.d0f = d_d0f.p;
     F.contact = d_contact.p;
     F.sig_a = d_sig_a.p;
     F.sig_b = d_sig_b.p;
@@ -193,6 +205,11 @@ struct ci_solver {
     F.status = d_status.p;
     F.bnd_final = bnd_final ? 1 : 0;
     F.store_acc = store_acc ? 1 : 0;
+    F.inst_ep = nullptr;
+    F.inst_np = nullptr;
+    F.inst_nsteps = nullptr;
+    F.step_ctr = nullptr;
+    F.step_off = 0;
     return F;
   }
   ci::NodeParams node_params() const {
@@ -201,6 +218,8 @@ struct ci_solver {
     for (int k = 0; k < 3; k++) {
       p.g[k] = opt.gravity[k];
       p.wall_n[k] = wall.normal[k];
+      p.gf[k] = (float)opt.gravity[k];
+      p.nf[k] = (float)wall.normal[k];
     }
     p.wall_k = wall.stiffness;
     p.N = N;
@@ -221,6 +240,14 @@ cudaError_t configure_step(int bytes) {
   cudaError_t e = cudaFuncSetAttribute(ci::k_step<NPE, ci::EM_J2, BS>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e) return e;
+  if (NPE == 10) {
+    if ((e = cudaFuncSetAttribute(ci::k_step_qp10<ci::EM_J2, BS>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+      return e;
+    if ((e = cudaFuncSetAttribute(ci::k_step_qp10<ci::EM_REFCOMPAT, BS>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+      return e;
+  }
   return cudaFuncSetAttribute(ci::k_step<NPE, ci::EM_REFCOMPAT, BS>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
@@ -249,6 +276,13 @@ cudaError_t configure_npe(int bytes) {
 template <int NPE, int BS>
 cudaError_t launch_fused_bs(ci_solver* s, const ci::FusedArgs& F, const ci::ElemParams& ep,
                             const ci::NodeParams& np) {
+  if (NPE == 10 && s->opt.elem_lanes == 4) {
+    if (s->opt.mode != CI_MODE_REFCOMPAT)
+      ci::k_step_qp10<ci::EM_J2, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
+    else
+      ci::k_step_qp10<ci::EM_REFCOMPAT, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
+    return cudaGetLastError();
+  }
   if (s->opt.mode != CI_MODE_REFCOMPAT)
     ci::k_step<NPE, ci::EM_J2, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
   else
@@ -363,6 +397,9 @@ int upload_reference(ci_solver* s) {
   CI_CUDA(cudaMemcpyAsync(s->d_lx0.p, lx0.data(), sizeof(float) * lx0.size(),
                           cudaMemcpyHostToDevice, s->stream));
   CI_CUDA(cudaMemcpyAsync(s->d_d0.p, d0.data(), sizeof(double) * d0.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  std::vector<float> d0f(d0.begin(), d0.end());
+  CI_CUDA(cudaMemcpyAsync(s->d_d0f.p, d0f.data(), sizeof(float) * d0f.size(), cudaMemcpyHostToDevice,
                           s->stream));
   CI_CUDA(cudaStreamSynchronize(s->stream));
   return CI_OK;
@@ -530,6 +567,9 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   if (s->opt.step_kernel != 0 && s->opt.step_kernel != 1)
     return fail(CI_ERR_INVALID, "unknown step_kernel");
   if (s->opt.block_threads == 0) s->opt.block_threads = 128;
+  if (s->opt.elem_lanes == 0) s->opt.elem_lanes = 4;
+  if (s->opt.elem_lanes != 1 && s->opt.elem_lanes != 4)
+    return fail(CI_ERR_INVALID, "elem_lanes must be 1 or 4");
   if (s->opt.block_threads != 64 && s->opt.block_threads != 128 && s->opt.block_threads != 256)
     return fail(CI_ERR_INVALID, "block_threads must be 64, 128 or 256");
   s->mat = *mat;
@@ -587,6 +627,7 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   }
   CI_CUDA(s->d_mass.alloc(N));
   CI_CUDA(s->d_d0.alloc(N));
+  CI_CUDA(s->d_d0f.alloc(N));
   CI_CUDA(s->d_contact.alloc(N));
   CI_CUDA(s->d_acc.alloc(3 * N));
   CI_CUDA(s->d_sig_a.alloc(E * s->nq));
@@ -634,8 +675,8 @@ int ci_start(ci_solver* s, double dt) {
   s->dt = dt;
   destroy_graph(s);
   if ((rc = compute_mass(s))) return rc;
-  ci::k_node<true, true><<<(s->N + 255) / 256, 256, 0, s->stream>>>(s->node_arrays(),
-                                                                    s->node_params());
+  ci::k_node_init<false><<<(s->N + 255) / 256, 256, 0, s->stream>>>(
+      s->node_arrays(), s->node_params(), nullptr, nullptr, s->d_d0f.p);
   CI_CUDA(cudaGetLastError());
   s->started = true;
   return check_status(s);
@@ -724,7 +765,7 @@ int ci_get_state(ci_solver* s, double* x, double* v, double* mass, float* sigma,
   for (int pe = 0; pe < E; pe++) {
     const int oe = P.elem_orig[pe];
     for (int q = 0; q < nq; q++) {
-      const size_t qi = (size_t)q * E + pe, o = (size_t)oe * nq + q;
+      const size_t qi = (size_t)pe * nq + q, o = (size_t)oe * nq + q;
       if (sigma) {
         const float4 a = hsa[qi];
         const float2 b = hsb[qi];
@@ -842,7 +883,7 @@ int ci_internal_force(ci_solver* s, const double* x, const double* du, const flo
     std::vector<float> ep((size_t)E * nq, 0.f);
     for (int pe = 0; pe < E; pe++)
       for (int q = 0; q < nq; q++) {
-        const size_t qi = (size_t)q * E + pe, o = (size_t)P.elem_orig[pe] * nq + q;
+        const size_t qi = (size_t)pe * nq + q, o = (size_t)P.elem_orig[pe] * nq + q;
         if (sigma_in) {
           const float* d = sigma_in + 6 * o;
           sa[qi] = make_float4(d[0], d[1], d[2], d[3]);
@@ -880,7 +921,7 @@ int ci_internal_force(ci_solver* s, const double* x, const double* du, const flo
     CI_CUDA(cudaMemcpy(ep.data(), s->d_epbar2.p, sizeof(float) * ep.size(), cudaMemcpyDeviceToHost));
     for (int pe = 0; pe < E; pe++)
       for (int q = 0; q < nq; q++) {
-        const size_t qi = (size_t)q * E + pe, o = (size_t)P.elem_orig[pe] * nq + q;
+        const size_t qi = (size_t)pe * nq + q, o = (size_t)P.elem_orig[pe] * nq + q;
         if (sigma_out) {
           float* d = sigma_out + 6 * o;
           d[0] = sa[qi].x; d[1] = sa[qi].y; d[2] = sa[qi].z; d[3] = sa[qi].w;

@@ -96,6 +96,8 @@ typedef struct ci_options {
   int graph_steps;    /* steps captured per CUDA graph, 0 = automatic */
   int step_kernel;    /* 0 = fused (one launch per step, default), 1 = element + node kernels */
   int block_threads;  /* threads per chunk CTA of the fused kernel: 64, 128 or 256; 0 = automatic */
+  int elem_lanes;     /* tet10 fused kernel: 4 = one lane per Gauss point, 1 = one thread per
+                         element; 0 = automatic (4) */
 } ci_options;
 
 /* energy terms (FP64), see ci_get_energy */
@@ -164,6 +166,34 @@ int ci_lumped_mass(ci_solver* s, const double* x, double* mass);
 /* Dynamics::debug_strain: total strain energy 1/2 u . K u and volume at the mesh
  * positions for a prescribed displacement u[3N] (RefCompat force). */
 int ci_strain_energy(ci_solver* s, const double* u, double* energy, double* volume);
+
+/* ---- batched solves: many instances of uneven size, one launch per step ----
+ * No reference counterpart (the reference solves one mesh per Dynamics object); the
+ * batch is the parameter-sweep form of ci_create + ci_initialize + ci_solve.  Every
+ * instance has its own mesh (tet4 or tet10), J2 material, wall, initial position
+ * offset and velocity, dt and end time; it runs the reference's loop count
+ * (while t <= t_end) with HRZ lumping, exactly as a single J2 solve with the same
+ * options (bitwise the same result).  Instances of each element type share one
+ * graph-captured launch per step; tet4 and tet10 groups run on two streams. */
+typedef struct ci_instance {
+  ci_mesh mesh;
+  ci_material mat;
+  ci_wall wall;
+  double pos[3];
+  double vel[3];
+  double dt;
+  double t_end;
+} ci_instance;
+typedef struct ci_batch ci_batch;
+int ci_batch_create(const ci_instance* inst, int n, const ci_options* opt, ci_batch** out);
+/* Runs every instance from its initial state to its end time; *device_ms (may be
+ * NULL) receives the device time of the whole batch (CUDA events). */
+int ci_batch_run(ci_batch* b, float* device_ms);
+/* Final state of instance i (caller order; any pointer may be NULL): x, v [3N],
+ * epbar [E*nq], contact [N] as ci_get_state, *nsteps the steps it ran. */
+int ci_batch_get_state(ci_batch* b, int i, double* x, double* v, float* epbar,
+                       unsigned char* contact, long long* nsteps);
+int ci_batch_destroy(ci_batch* b);
 
 /* ---- timing helpers for benchmarks (CUDA events on the solver's stream) ---- */
 int ci_time_steps(ci_solver* s, int nsteps, float* ms);
