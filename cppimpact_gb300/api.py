@@ -93,6 +93,9 @@ EXPORTS = {
     "ci_plan_stats": (C.c_int, [C.POINTER(CiMesh), C.c_int, C.c_int, C.POINTER(C.c_longlong),
                                 _ip, _ip]),
     "ci_plan_verify": (C.c_int, [C.POINTER(CiMesh), C.c_int, C.c_int]),
+    "ci_strain_energy_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                           C.c_void_p, C.c_double, C.c_double, C.c_void_p,
+                                           C.c_void_p]),
 }
 
 

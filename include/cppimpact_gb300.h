@@ -195,6 +195,28 @@ int ci_batch_get_state(ci_batch* b, int i, double* x, double* v, float* epbar,
                        unsigned char* contact, long long* nsteps);
 int ci_batch_destroy(ci_batch* b);
 
+/* ---- allocation-free variant (no counterpart in the reference) ----
+ * ci_strain_energy_noalloc computes what ci_strain_energy computes -- the total strain
+ * energy 1/2 u.K u and the volume of a mesh for a prescribed displacement -- without
+ * allocating anything, for callers that cannot call cudaMalloc: programs that own all
+ * device memory through their own pool and forbid driver allocations after start-up,
+ * plug-ins living inside such programs, and time-critical loops that must not incur
+ * cudaMalloc's synchronisation or its failure under memory pressure.  It needs no
+ * solver: d_xloc [3N] and d_u [3N] (FP64), d_element_nodes [npe*E] (int) and d_out [2]
+ * (energy, volume; FP64) are device buffers the caller owns; the work is enqueued on
+ * `stream` (a cudaStream_t, NULL = the legacy default stream) and the result is in
+ * d_out once that stream reaches it.  Its scratch is a fixed array compiled into the
+ * library (CI_NOALLOC_MAX_ELEMENTS / 256 blocks x 2 doubles = 256 KiB on every GPU the
+ * library is used on), so at most CI_NOALLOC_MAX_ELEMENTS elements are accepted
+ * (CI_ERR_TOO_LARGE beyond).  The first call on each device looks up the scratch's
+ * device address and should happen before any stream capture.  Calls share the
+ * scratch: calls that can overlap on the GPU race and must be serialised by the
+ * caller.  A non-positive det J makes the energy NaN. */
+#define CI_NOALLOC_MAX_ELEMENTS (1 << 22)
+int ci_strain_energy_noalloc(const double* d_xloc, const int* d_element_nodes, int num_nodes,
+                             int num_elements, int nodes_per_element, const double* d_u, double E,
+                             double nu, double* d_out, void* stream);
+
 /* ---- timing helpers for benchmarks (CUDA events on the solver's stream) ---- */
 int ci_time_steps(ci_solver* s, int nsteps, float* ms);
 /* Runs nsteps steps launching each kernel between CUDA events and returns mean device
