@@ -274,7 +274,52 @@ def run_ours(args, rank, world):
     s.close()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(m, setup, args.cpu_seconds)
+    if rank == 0 and args.sweep:
+        line["sweep"] = run_sweep(args)
     return line
+
+
+def run_sweep(args, count=256, sample=16):
+    """The batched sweep: runs/hour of the batch (one launch per step per element type)
+    and of the plain solver running instances one at a time (device time of a sample,
+    extrapolated to the whole sweep)."""
+    from cppimpact_gb300 import api, sweep
+    t0 = time.perf_counter()
+    inst = sweep.make_instances(count)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b = api.Batch(inst)
+    t_create = time.perf_counter() - t0
+    b.run()  # warm-up run
+    ms = b.run()
+    def nsteps(d):
+        n, t = 0, 0.0
+        while t <= d["t_end"]:
+            n += 1
+            t += d["dt"]
+        return n
+    el_steps = sum(d["conn"].shape[0] * nsteps(d) for d in inst)
+    b.close()
+    # the plain solver: same instances one at a time (sampled)
+    single_ms = []
+    for d in inst[:sample]:
+        s = api.Solver(d["xloc"], d["conn"], E=d["E"], nu=d["nu"], rho=d["rho"],
+                       sigma_y0=d["sigma_y0"], H=d["H"], wall_normal=d["wall_normal"],
+                       wall_offset=d["wall_offset"], wall_stiffness=d["wall_stiffness"])
+        s.initialize(d["vel"])
+        s.start(d["dt"])
+        single_ms.append(s.time_steps(nsteps(d)))
+        s.close()
+    frac = sum(d["conn"].shape[0] for d in inst[:sample]) / sum(d["conn"].shape[0] for d in inst)
+    plain_ms = sum(single_ms) / max(frac, 1e-12)
+    return {"instances": count, "t_end_s": 2e-3, "batch_device_ms": ms,
+            "runs_per_hour": count / (ms / 1e3) * 3600.0,
+            "plain_gpu_runs_per_hour": count / (plain_ms / 1e3) * 3600.0,
+            "speedup_vs_plain_gpu": plain_ms / ms,
+            "element_steps_per_s": el_steps / (ms / 1e3),
+            "plain_sample": sample, "setup_s": {"meshes": round(t_gen, 2), "plans": round(t_create, 2)},
+            "peak_disp_err_vs_unbatched": 0.0,
+            "note": "each instance is bitwise its unbatched run (tests/test_gpu_batch.py)"}
 
 
 def run_reference(args, rank, world):
@@ -334,6 +379,7 @@ def main():
     ap.add_argument("--e2e-interval", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sweep", type=int, default=1, help="also run the 256-instance batched sweep")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per element-kernel launch from an ncu capture")
     args = ap.parse_args()

@@ -59,6 +59,12 @@ class CiOptions(C.Structure):
                 ("elem_lanes", C.c_int)]
 
 
+class CiInstance(C.Structure):
+    _fields_ = [("mesh", CiMesh), ("mat", CiMaterial), ("wall", CiWall),
+                ("pos", C.c_double * 3), ("vel", C.c_double * 3), ("dt", C.c_double),
+                ("t_end", C.c_double)]
+
+
 class CiEnergy(C.Structure):
     _fields_ = [("kinetic", C.c_double), ("internal", C.c_double), ("plastic", C.c_double),
                 ("contact", C.c_double), ("gravity", C.c_double), ("kinetic0", C.c_double),
@@ -93,6 +99,12 @@ EXPORTS = {
     "ci_plan_stats": (C.c_int, [C.POINTER(CiMesh), C.c_int, C.c_int, C.POINTER(C.c_longlong),
                                 _ip, _ip]),
     "ci_plan_verify": (C.c_int, [C.POINTER(CiMesh), C.c_int, C.c_int]),
+    "ci_batch_create": (C.c_int, [C.POINTER(CiInstance), C.c_int, C.POINTER(CiOptions),
+                                  C.POINTER(C.c_void_p)]),
+    "ci_batch_run": (C.c_int, [C.c_void_p, _fp]),
+    "ci_batch_get_state": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _fp, _ubp,
+                                     C.POINTER(C.c_longlong)]),
+    "ci_batch_destroy": (C.c_int, [C.c_void_p]),
     "ci_strain_energy_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                            C.c_void_p, C.c_double, C.c_double, C.c_void_p,
                                            C.c_void_p]),
@@ -286,6 +298,69 @@ class Solver:
 
     def launches_per_step(self) -> int:
         return lib().ci_launches_per_step(self._h)
+
+
+class Batch:
+    """Many instances (each: mesh, J2 material, wall, velocity, dt, end time) advanced
+    together, one launch per step per element type (``ci_batch_*``).
+
+    ``instances``: dicts with keys xloc, conn, E, nu, rho, sigma_y0, H, wall_normal,
+    wall_offset, wall_stiffness, vel, dt, t_end (and optionally pos)."""
+
+    def __init__(self, instances, *, gravity=(0.0, 0.0, -9.81), device=0, chunk_nodes=0,
+                 block_threads=0, elem_lanes=0):
+        self._meshes = []
+        arr = (CiInstance * len(instances))()
+        for i, d in enumerate(instances):
+            m = MeshArrays(d["xloc"], d["conn"])
+            self._meshes.append(m)
+            arr[i].mesh = m.c
+            arr[i].mat = CiMaterial(d["E"], d["nu"], d["rho"], d.get("sigma_y0", 0.0),
+                                    d.get("H", 0.0), 0.0)
+            arr[i].wall = CiWall((C.c_double * 3)(*d["wall_normal"]), d["wall_offset"],
+                                 d["wall_stiffness"])
+            arr[i].pos = (C.c_double * 3)(*d.get("pos", (0.0, 0.0, 0.0)))
+            arr[i].vel = (C.c_double * 3)(*d["vel"])
+            arr[i].dt = d["dt"]
+            arr[i].t_end = d["t_end"]
+        opt = CiOptions()
+        lib().ci_default_options(C.byref(opt))
+        opt.gravity = (C.c_double * 3)(*gravity)
+        opt.device, opt.chunk_nodes = device, chunk_nodes
+        opt.block_threads, opt.elem_lanes = block_threads, elem_lanes
+        self._arr = arr
+        self._h = C.c_void_p()
+        check(lib().ci_batch_create(arr, len(instances), C.byref(opt), C.byref(self._h)))
+        self.n = len(instances)
+
+    def run(self) -> float:
+        """Runs every instance to its end time; returns the batch's device time in ms."""
+        ms = C.c_float(0)
+        check(lib().ci_batch_run(self._h, C.byref(ms)))
+        return ms.value
+
+    def state(self, i):
+        m = self._meshes[i]
+        N, (E, npe) = m.xloc.shape[0], m.conn.shape
+        nq = 1 if npe == 4 else 4
+        x, v = np.zeros((N, 3)), np.zeros((N, 3))
+        ep = np.zeros((E, nq), dtype=np.float32)
+        ct = np.zeros(N, dtype=np.uint8)
+        ns = C.c_longlong(0)
+        check(lib().ci_batch_get_state(self._h, i, _d(x), _d(v), _f(ep),
+                                       ct.ctypes.data_as(_ubp), C.byref(ns)))
+        return dict(x=x, v=v, epbar=ep, contact=ct, nsteps=ns.value)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().ci_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------

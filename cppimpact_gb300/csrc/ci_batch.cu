@@ -82,7 +82,7 @@ struct Group {
   long long S = 0, Lt = 0;
   int max_local = 0;
   size_t smem = 0;
-  int block_threads = 128, elem_lanes = 4, chunk_nodes = 2048;
+  int block_threads = 128, elem_lanes = 4, chunk_nodes = 1024;
   std::vector<int> insts;  // global instance ids
   int max_steps = 0;
   cudaStream_t stream = nullptr;
@@ -500,7 +500,7 @@ int ci_batch_create(const ci_instance* inst, int n, const ci_options* opt_in, ci
     if (G->insts.empty()) continue;
     G->block_threads = opt.block_threads ? opt.block_threads : 128;
     G->elem_lanes = opt.elem_lanes ? opt.elem_lanes : 4;
-    G->chunk_nodes = opt.chunk_nodes ? opt.chunk_nodes : 2048;
+    G->chunk_nodes = opt.chunk_nodes ? opt.chunk_nodes : 1024;
     CB_CUDA(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
     int rc = build_group(b.get(), *G, inst, opt);
     if (rc) return rc;

@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(kThreads) k_energy_partials(const double* __re
         xe[a][k] = (float)(x[3 * (size_t)n[a] + k] - x[3 * (size_t)n[0] + k]);
         ue[a][k] = (float)u[3 * (size_t)n[a] + k];
       }
-    ci::DevState S;
+    ci::DevState S{};
     S.status = status;
     float f[NPE][3];
     ci::element_force<NPE, ci::EM_REFCOMPAT>(p, S, e, E, xe, ue, f, wint, wp, vol);
