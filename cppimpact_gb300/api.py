@@ -105,6 +105,22 @@ EXPORTS = {
     "ci_batch_get_state": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _fp, _ubp,
                                      C.POINTER(C.c_longlong)]),
     "ci_batch_destroy": (C.c_int, [C.c_void_p]),
+    "ci_batch_run_snapshots": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, _fp]),
+    "ci_batch_node_order": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip]),
+    "ci_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    "ci_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "ci_mlp_num_params": (C.c_longlong, [C.c_void_p]),
+    "ci_mlp_set_params": (C.c_int, [C.c_void_p, _fp]),
+    "ci_mlp_get_params": (C.c_int, [C.c_void_p, _fp]),
+    "ci_mlp_predict": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "ci_mlp_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _fp,
+                                   C.POINTER(C.c_double)]),
+    "ci_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                               C.c_float, C.c_ulonglong, _dp, C.c_void_p]),
+    "ci_gemm_bf16": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                               C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                               C.c_float, C.c_float, C.c_void_p, C.c_int, C.c_void_p,
+                               C.c_void_p]),
     "ci_strain_energy_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                            C.c_void_p, C.c_double, C.c_double, C.c_void_p,
                                            C.c_void_p]),
@@ -338,6 +354,20 @@ class Batch:
         ms = C.c_float(0)
         check(lib().ci_batch_run(self._h, C.byref(ms)))
         return ms.value
+
+    def run_snapshots(self, every, d_snap_ptr, max_snaps) -> float:
+        """Run with displacement snapshots (device buffer [max_snaps][N_total][3] FP32)."""
+        ms = C.c_float(0)
+        check(lib().ci_batch_run_snapshots(self._h, int(every), C.c_void_p(d_snap_ptr),
+                                           int(max_snaps), C.byref(ms)))
+        return ms.value
+
+    def node_order(self, i):
+        m = self._meshes[i]
+        perm = np.zeros(m.xloc.shape[0], dtype=np.int32)
+        off = C.c_int(0)
+        check(lib().ci_batch_node_order(self._h, i, perm.ctypes.data_as(_ip), C.byref(off)))
+        return perm, off.value
 
     def state(self, i):
         m = self._meshes[i]

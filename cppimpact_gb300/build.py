@@ -21,7 +21,7 @@ LIB = os.path.join(PKG, "libcppimpact_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["ci_plan.cpp", "ci_inp.cpp"]
-CUDA_SOURCES = ["ci_solver.cu", "ci_batch.cu", "ci_noalloc.cu"]
+CUDA_SOURCES = ["ci_solver.cu", "ci_batch.cu", "ci_gemm.cu", "ci_mlp.cu", "ci_noalloc.cu"]
 
 
 def _nvcc() -> str:

@@ -93,6 +93,7 @@ struct Group {
   DBuf<int> lgid, lslot, slot_row, bnd, node_inst;
   DBuf<float> lx0, slot0, slot1, mass, d0f, acc, epbar, peak;
   DBuf<double> ua, va, ub, vb, v0, d0, work;
+  DBuf<float> ufa, vfa, ufb, vfb;  // FP32 copies of the state buffers
   DBuf<unsigned char> contact;
   DBuf<float4> sig_a;
   DBuf<float2> sig_b;
@@ -169,6 +170,10 @@ FusedArgs group_args(const Group& G, int i_in_graph) {
     F.v_cur[k] = (even ? G.va.p : G.vb.p) + k * N;
     F.u_prv[k] = (even ? G.ub.p : G.ua.p) + k * N;
     F.v_prv[k] = (even ? G.vb.p : G.va.p) + k * N;
+    F.uf_cur[k] = (even ? G.ufa.p : G.ufb.p) + k * N;
+    F.vf_cur[k] = (even ? G.vfa.p : G.vfb.p) + k * N;
+    F.uf_prv[k] = (even ? G.ufb.p : G.ufa.p) + k * N;
+    F.vf_prv[k] = (even ? G.vfb.p : G.vfa.p) + k * N;
     F.halo_cur[k] = (even ? G.slot0.p : G.slot1.p) + k * S;
     F.halo_prv[k] = (even ? G.slot1.p : G.slot0.p) + k * S;
     F.acc[k] = G.acc.p + k * N;
@@ -325,7 +330,7 @@ int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& 
   }
   slot_row.push_back((int)s_off);
   G.n_bnd = (int)bnd.size();
-  G.smem = sizeof(float) * 9 * (size_t)G.max_local;
+  G.smem = 40 * ((size_t)G.max_local + 2);
   cudaStream_t st = G.stream;
   CB_CUDA(G.chunks.upload(chunks, st));
   CB_CUDA(G.conn.upload(conn, st));
@@ -347,6 +352,10 @@ int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& 
   CB_CUDA(G.ua.alloc(3 * N));
   CB_CUDA(G.ub.alloc(3 * N));
   CB_CUDA(G.vb.alloc(3 * N));
+  CB_CUDA(G.ufa.alloc(3 * N));
+  CB_CUDA(G.vfa.alloc(3 * N));
+  CB_CUDA(G.ufb.alloc(3 * N));
+  CB_CUDA(G.vfb.alloc(3 * N));
   CB_CUDA(G.slot0.alloc(3 * (size_t)G.S));
   CB_CUDA(G.slot1.alloc(3 * (size_t)G.S));
   CB_CUDA(G.mass.alloc(N));
@@ -387,8 +396,9 @@ int capture_graph(Group& G) {
   return CI_OK;
 }
 
-// Reset to the initial state, lumped mass, a0 and half step; then enqueue all steps.
-int enqueue_run(Group& G) {
+// Reset to the initial state, lumped mass, a0 and half step; then (if launch) all
+// steps with the plain graph.
+int enqueue_run(Group& G, bool launch = true) {
   cudaStream_t st = G.stream;
   const size_t N = G.N, E = G.E;
   CB_CUDA(cudaMemsetAsync(G.ua.p, 0, sizeof(double) * 3 * N, st));
@@ -444,10 +454,70 @@ int enqueue_run(Group& G) {
   k_node_init<true><<<(G.N + 255) / 256, 256, 0, st>>>(A, np0, G.inst_np.p, G.node_inst.p,
                                                        G.d0f.p);
   CB_CUDA(cudaGetLastError());
-  // all global steps: max_steps + 1 (the last instance's boundary finalisation)
-  const int total = G.max_steps + 1;
-  for (int done = 0; done < total; done += kGraphSteps) CB_CUDA(cudaGraphLaunch(G.graph, st));
+  k_shadows<<<(unsigned)((3 * N + 255) / 256), 256, 0, st>>>(G.ua.p, G.va.p, G.ufa.p, G.vfa.p,
+                                                            3 * (long long)N);
+  CB_CUDA(cudaGetLastError());
+  if (launch) {
+    // all global steps: max_steps + 1 (the last instance's boundary finalisation)
+    const int total = G.max_steps + 1;
+    for (int done = 0; done < total; done += kGraphSteps) CB_CUDA(cudaGraphLaunch(G.graph, st));
+  }
   return CI_OK;
+}
+
+// enqueue_run's preparation, then graphs of `per_graph` steps covering `total` steps
+int enqueue_run_graph(Group& G, int total, int per_graph) {
+  const int rc = enqueue_run(G, false);
+  if (rc) return rc;
+  for (int done = 0; done < total; done += per_graph) CB_CUDA(cudaGraphLaunch(G.graph, G.stream));
+  return CI_OK;
+}
+
+// Displacement of every node after k = *step_ctr global steps, FP32, into
+// snap[(k / every - 1)][node][3] (plan order).  Interior nodes of an instance still
+// stepping hold S^k in buffer k & 1; its boundary nodes are completed from S^{k-1} and
+// the halo of step k-1 exactly as the next step would; instances that have finished
+// (k > nsteps) hold their final state in buffer nsteps & 1.
+__global__ void k_snapshot(FusedArgs A0, FusedArgs A1, const int* node_inst,
+                           const unsigned char* is_bnd, int N, int every, float* snap,
+                           int max_snaps) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int k = *A0.step_ctr;
+  const int si = k / every - 1;
+  if (si < 0 || si >= max_snaps) return;
+  const int inst = node_inst[n];
+  const int ns = A0.inst_nsteps[inst];
+  // A0: views with cur = buffer A (even k), A1: cur = buffer B
+  double u[3];
+  if (k > ns) {
+    const FusedArgs& F = (ns & 1) ? A1 : A0;
+    for (int c = 0; c < 3; c++) u[c] = F.u_cur[c][n];
+  } else if (!is_bnd[n]) {
+    const FusedArgs& F = (k & 1) ? A1 : A0;
+    for (int c = 0; c < 3; c++) u[c] = F.u_cur[c][n];
+  } else {
+    // halo_prv of the step-k view is the halo of step k-1
+    const FusedArgs& F = (k & 1) ? A1 : A0;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    for (int s = F.P.slot_row[n]; s < F.P.slot_row[n + 1]; s++) {
+      fx = __fadd_rn(fx, F.halo_prv[0][s]);
+      fy = __fadd_rn(fy, F.halo_prv[1][s]);
+      fz = __fadd_rn(fz, F.halo_prv[2][s]);
+    }
+    double v[3];
+    for (int c = 0; c < 3; c++) {
+      u[c] = F.u_prv[c][n];
+      v[c] = F.v_prv[c][n];
+    }
+    float a[3], uf[3], vf[3];
+    bool hit;
+    node_step(F.inst_np[inst], fx, fy, fz, F.mass[n], F.d0f[n], F.d0, n, u, v, a, hit, uf, vf);
+  }
+  float* o = snap + ((size_t)si * N + n) * 3;
+  o[0] = (float)u[0];
+  o[1] = (float)u[1];
+  o[2] = (float)u[2];
 }
 
 }  // namespace
@@ -585,6 +655,78 @@ int ci_batch_get_state(ci_batch* b, int i, double* x, double* v, float* epbar,
       for (int q = 0; q < nq; q++)
         epbar[(size_t)T.elem_orig[pe] * nq + q] = hep[(size_t)pe * nq + q];
   if (nsteps) *nsteps = T.nsteps;
+  return CI_OK;
+}
+
+int ci_batch_run_snapshots(ci_batch* b, int every, float* d_snap, int max_snaps, float* device_ms) {
+  if (!b || every <= 0 || (every & 1) || !d_snap || max_snaps <= 0)
+    return fail(CI_ERR_INVALID, "ci_batch_run_snapshots: needs an even interval and a buffer");
+  if (b->g[0] && b->g[1])
+    return fail(CI_ERR_UNSUPPORTED, "ci_batch_run_snapshots: one element type per batch");
+  CB_CUDA(cudaSetDevice(b->device));
+  Group& G = *(b->g[0] ? b->g[0] : b->g[1]);
+  // graph: `every` steps, then the snapshot of the state after them, then the tick
+  if (G.graph) cudaGraphExecDestroy(G.graph);
+  G.graph = nullptr;
+  std::vector<unsigned char> isb(G.N, 0);
+  {
+    std::vector<int> sr(G.N + 1);
+    CB_CUDA(cudaMemcpy(sr.data(), G.slot_row.p, sizeof(int) * (G.N + 1), cudaMemcpyDeviceToHost));
+    for (int n = 0; n < G.N; n++) isb[n] = sr[n + 1] - sr[n] > 1;
+  }
+  DBuf<unsigned char> d_isb;
+  CB_CUDA(d_isb.upload(isb, G.stream));
+  cudaGraph_t g = nullptr;
+  CB_CUDA(cudaStreamBeginCapture(G.stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t err = cudaSuccess;
+  for (int i = 0; i < every && err == cudaSuccess; i++) {
+    const FusedArgs F = group_args(G, i);
+    err = G.npe == 4 ? launch_batch<4>(G, F) : launch_batch<10>(G, F);
+  }
+  if (err == cudaSuccess) {
+    k_tick<<<1, 1, 0, G.stream>>>(G.step_ctr.p, every);
+    k_snapshot<<<(G.N + 255) / 256, 256, 0, G.stream>>>(group_args(G, 0), group_args(G, 1),
+                                                        G.node_inst.p, d_isb.p, G.N, every, d_snap,
+                                                        max_snaps);
+    err = cudaGetLastError();
+  }
+  cudaError_t e2 = cudaStreamEndCapture(G.stream, &g);
+  if (err != cudaSuccess || e2 != cudaSuccess)
+    return fail(CI_ERR_CUDA, std::string("snapshot capture: ") +
+                                 cudaGetErrorString(err != cudaSuccess ? err : e2));
+  err = cudaGraphInstantiate(&G.graph, g, 0);
+  cudaGraphDestroy(g);
+  if (err != cudaSuccess) return fail(CI_ERR_CUDA, std::string("snapshot graph: ") + cudaGetErrorString(err));
+  CB_CUDA(cudaEventRecord(b->ev0, G.stream));
+  // enqueue_run launches ceil((max_steps + 1) / every) graphs of `every` steps
+  {
+    const int total = G.max_steps + 1;
+    cudaStream_t st = G.stream;
+    // same preparation as a normal run, with the snapshot graph
+    const int rc = enqueue_run_graph(G, total, every);
+    if (rc) return rc;
+    (void)st;
+  }
+  CB_CUDA(cudaEventRecord(b->ev1, G.stream));
+  CB_CUDA(cudaEventSynchronize(b->ev1));
+  CB_CUDA(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1));
+  if (device_ms) *device_ms = b->last_ms;
+  // restore the plain graph for later ci_batch_run calls
+  const int rc = capture_graph(G);
+  if (rc) return rc;
+  unsigned int stw = 0;
+  CB_CUDA(cudaMemcpy(&stw, G.status.p, sizeof(stw), cudaMemcpyDeviceToHost));
+  if (stw & ST_NONFINITE) return fail(CI_ERR_NONFINITE, "non-finite nodal state");
+  b->done = true;
+  return CI_OK;
+}
+
+/* Plan order of instance i's nodes: perm[p] = caller node of plan node p. */
+int ci_batch_node_order(ci_batch* b, int i, int* perm, int* node_offset) {
+  if (!b || i < 0 || i >= (int)b->inst.size() || !perm) return fail(CI_ERR_INVALID, "bad argument");
+  const Inst& T = b->inst[i];
+  std::memcpy(perm, T.node_orig.data(), sizeof(int) * T.N);
+  if (node_offset) *node_offset = T.node_off;
   return CI_OK;
 }
 

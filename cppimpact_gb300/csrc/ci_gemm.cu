@@ -1,0 +1,285 @@
+// ci_gemm.cu -- BF16 tensor-core GEMM on sm_103a (tcgen05 + TMEM), FP32 accumulation.
+//
+//   C[M x N] (+)= alpha * op(A)[M x K] * op(B)[K x N]  (+ bias[N]) (then optional tanh)
+//
+// A, B are BF16 in global memory, row-major with leading dimensions lda/ldb; op() is a
+// transpose flag per operand.  C is FP32 (row-major, ldc); an optional BF16 copy of C
+// is written for the next layer.  This is the dense contraction of the surrogate (POD
+// projections and the MLP's forward/backward passes); the impact step itself has none.
+//
+// One CTA computes a 128 x BN tile (BN = 64 or 128).  Per K-tile of 64:
+//  1. all 128 threads stage A (128 x 64) and B (BN x 64) as K-major BF16 in shared
+//     memory, in the canonical no-swizzle layout of 8-row x 16-byte core matrices
+//     (core matrix (r/8, k/8) at r/8 * SBO + k/8 * LBO, LBO = 128 B, SBO = 1024 B);
+//  2. fence.proxy.async makes the writes visible to the tensor core; one elected
+//     thread issues 4 x tcgen05.mma.kind::f16 (K = 16 each) into the TMEM accumulator
+//     and commits to an mbarrier;
+//  3. every thread waits on the mbarrier (bounded spin: on timeout the kernel records
+//     an error flag, frees its TMEM and returns) before the stage is overwritten.
+// The epilogue reads the accumulator with tcgen05.ld (each warp its 32 TMEM lanes =
+// 32 rows), applies alpha, beta, bias, tanh and stores.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <string>
+
+#include "../../include/cppimpact_gb300.h"
+
+namespace ci {
+int set_last_error(int code, const char* msg);
+}
+
+namespace {
+
+constexpr int BM = 128;
+constexpr int BK = 64;
+constexpr unsigned kSpinLimit = 1u << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// tcgen05 shared-memory matrix descriptor: start address, leading / stride byte
+// offsets (all >> 4), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // version
+  return d;                // base offset 0, lbo mode 0, layout 0 (no swizzle)
+}
+
+// Instruction descriptor of tcgen05.mma.kind::f16: D FP32, A and B BF16, both K-major,
+// N >> 3 and M >> 4.
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
+  return (1u << 4)      // D format F32
+         | (1u << 7)    // A format BF16
+         | (1u << 10)   // B format BF16
+         | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+  for (unsigned it = 0; it < kSpinLimit; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// byte offset of element (r, k) of a K-major no-swizzle tile (LBO 128, SBO 1024)
+__device__ __forceinline__ uint32_t kmajor_off(int r, int k) {
+  return (uint32_t)((r >> 3) * 1024 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+template <int BN>
+__global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16* __restrict__ A, int lda,
+                                                   int transA, const __nv_bfloat16* __restrict__ B,
+                                                   int ldb, int transB, float* C, int ldc,
+                                                   __nv_bfloat16* Cb, int M, int N, int K,
+                                                   float alpha, float beta,
+                                                   const float* __restrict__ bias, int act,
+                                                   int* err, int k_chunk, float* partial) {
+  __shared__ __align__(1024) uint8_t sA[BM * BK * 2];
+  __shared__ __align__(1024) uint8_t sB[BN * BK * 2];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  // split-K: this CTA reduces K range [kb, ke); partial results go to partial[z]
+  const int kb = blockIdx.z * k_chunk;
+  const int ke = min(K, kb + k_chunk);
+
+  if (warp == 0) {
+    // TMEM: BN columns (power of two >= 32) for the 128 x BN FP32 accumulator
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  const uint32_t idesc = instr_desc(BM, BN);
+  bool ok = true;
+  uint32_t phase = 0;
+  const int ktiles = (ke - kb + BK - 1) / BK;
+  for (int kt = 0; kt < ktiles && ok; kt++) {
+    const int k0 = kb + kt * BK;
+    // stage A: 128 rows x 64 k; consecutive threads read consecutive addresses
+    for (int i = tid; i < BM * BK; i += 128) {
+      const int r = transA ? i % BM : i / BK, k = transA ? i / BM : i % BK;
+      const int gm = m0 + r, gk = k0 + k;
+      __nv_bfloat16 v = __float2bfloat16(0.f);
+      if (gm < M && gk < ke) v = transA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
+      *reinterpret_cast<__nv_bfloat16*>(sA + kmajor_off(r, k)) = v;
+    }
+    // stage B as K-major rows n: B_op[k][n]
+    for (int i = tid; i < BN * BK; i += 128) {
+      const int n = transB ? i / BK : i % BN, k = transB ? i % BK : i / BN;
+      const int gn = n0 + n, gk = k0 + k;
+      __nv_bfloat16 v = __float2bfloat16(0.f);
+      if (gn < N && gk < ke) v = transB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
+      *reinterpret_cast<__nv_bfloat16*>(sB + kmajor_off(n, k)) = v;
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; kk++) {
+        // K = 16 per MMA = two core matrices along K = 2 x LBO bytes
+        const uint64_t da = smem_desc(smem_u32(sA) + kk * 256, 128, 1024);
+        const uint64_t db = smem_desc(smem_u32(sB) + kk * 256, 128, 1024);
+        const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+              smem_u32(&bar))
+          : "memory");
+    }
+    // CTA-uniform outcome: every thread leaves the loop at the same tile
+    ok = __syncthreads_and(mbar_wait(smem_u32(&bar), phase)) != 0;
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  }
+  if (!ok) {
+    // give the MMAs in flight one more bounded wait before the TMEM is freed
+    mbar_wait(smem_u32(&bar), phase ^ 1u);
+    if (tid == 0) atomicExch(err, 1);
+  } else {
+    // epilogue: warp w holds TMEM lanes [32w, 32w+32) = tile rows; 8 columns per load
+    const int row = m0 + warp * 32 + lane;
+    for (int c = 0; c < BN; c += 8) {
+      uint32_t r[8];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (row < M && partial) {
+        float* pr = partial + ((size_t)blockIdx.z * M + row) * N;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+          if (n0 + c + j < N) pr[n0 + c + j] = ktiles > 0 ? __uint_as_float(r[j]) : 0.f;
+      } else if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int col = n0 + c + j;
+          if (col >= N) continue;
+          float v = alpha * __uint_as_float(r[j]);
+          if (beta != 0.f) v += beta * C[(size_t)row * ldc + col];
+          if (bias) v += bias[col];
+          if (act == 1) v = tanhf(v);
+          C[(size_t)row * ldc + col] = v;
+          if (Cb) Cb[(size_t)row * ldc + col] = __float2bfloat16(v);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN)
+                 : "memory");
+}
+
+// C = alpha sum_z partial[z] (z in order) + beta C + bias, then tanh; BF16 copy.
+__global__ void k_splitk_reduce(const float* partial, int splits, float* C, int ldc,
+                                __nv_bfloat16* Cb, int M, int N, float alpha, float beta,
+                                const float* bias, int act) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)M * N) return;
+  const int row = (int)(i / N), col = (int)(i % N);
+  float acc = 0.f;
+  for (int z = 0; z < splits; z++) acc += partial[(size_t)z * M * N + i];
+  float v = alpha * acc;
+  if (beta != 0.f) v += beta * C[(size_t)row * ldc + col];
+  if (bias) v += bias[col];
+  if (act == 1) v = tanhf(v);
+  C[(size_t)row * ldc + col] = v;
+  if (Cb) Cb[(size_t)row * ldc + col] = __float2bfloat16(v);
+}
+
+// split-K workspace, grown on demand, one per device
+float* g_ws[64] = {};
+size_t g_ws_size[64] = {};
+
+}  // namespace
+
+extern "C" int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, int ldb, int transB,
+                            float* C, int ldc, void* C_bf16, int M, int N, int K, float alpha,
+                            float beta, const float* bias, int activation, int* d_error,
+                            void* stream) {
+  if (!A || !B || !C || !d_error || M <= 0 || N <= 0 || K <= 0)
+    return ci::set_last_error(CI_ERR_INVALID, "ci_gemm_bf16: null pointer or empty shape");
+  if (activation != 0 && activation != 1)
+    return ci::set_last_error(CI_ERR_INVALID, "ci_gemm_bf16: activation must be 0 or 1");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int bn = N <= 64 ? 64 : 128;
+  const int tiles = ((M + BM - 1) / BM) * ((N + bn - 1) / bn);
+  // split K when the output has too few tiles to fill the GPU and K is long
+  int splits = 1;
+  if (tiles < 304 && K >= 8 * BK) splits = std::min((304 + tiles - 1) / tiles, (K + 4 * BK - 1) / (4 * BK));
+  splits = std::max(1, std::min(splits, 512));
+  int k_chunk = (K + splits - 1) / splits;
+  k_chunk = (k_chunk + BK - 1) / BK * BK;
+  splits = (K + k_chunk - 1) / k_chunk;
+  float* partial = nullptr;
+  if (splits > 1) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const size_t need = sizeof(float) * (size_t)splits * M * N;
+    if (dev < 0 || dev >= 64) return ci::set_last_error(CI_ERR_CUDA, "ci_gemm_bf16: bad device");
+    if (g_ws_size[dev] < need) {
+      if (g_ws[dev]) cudaFree(g_ws[dev]);
+      g_ws[dev] = nullptr;
+      g_ws_size[dev] = 0;
+      if (cudaMalloc(&g_ws[dev], need) != cudaSuccess)
+        return ci::set_last_error(CI_ERR_NOMEM, "ci_gemm_bf16: split-K workspace");
+      g_ws_size[dev] = need;
+    }
+    partial = g_ws[dev];
+  }
+  dim3 grid((M + BM - 1) / BM, (N + bn - 1) / bn, splits);
+  if (bn == 64)
+    k_gemm_bf16<64><<<grid, 128, 0, st>>>(
+        static_cast<const __nv_bfloat16*>(A), lda, transA, static_cast<const __nv_bfloat16*>(B),
+        ldb, transB, C, ldc, static_cast<__nv_bfloat16*>(C_bf16), M, N, K, alpha, beta, bias,
+        activation, d_error, k_chunk, partial);
+  else
+    k_gemm_bf16<128><<<grid, 128, 0, st>>>(
+        static_cast<const __nv_bfloat16*>(A), lda, transA, static_cast<const __nv_bfloat16*>(B),
+        ldb, transB, C, ldc, static_cast<__nv_bfloat16*>(C_bf16), M, N, K, alpha, beta, bias,
+        activation, d_error, k_chunk, partial);
+  if (splits > 1) {
+    const long long mn = (long long)M * N;
+    k_splitk_reduce<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(
+        partial, splits, C, ldc, static_cast<__nv_bfloat16*>(C_bf16), M, N, alpha, beta, bias,
+        activation);
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return ci::set_last_error(CI_ERR_CUDA, cudaGetErrorString(e));
+  return CI_OK;
+}

@@ -468,6 +468,12 @@ struct FusedArgs {
   double* v_cur[3];
   double* u_prv[3];
   double* v_prv[3];
+  // FP32 copies of u and v, double-buffered with them: staging reads these, so the
+  // FP64 state is converted once per update instead of at every staging
+  float* uf_cur[3];
+  float* vf_cur[3];
+  float* uf_prv[3];
+  float* vf_prv[3];
   const float* halo_prv[3];
   float* halo_cur[3];
   const float* mass;
@@ -529,7 +535,8 @@ __device__ __forceinline__ ChunkStep chunk_step(const FusedArgs& A, const ChunkI
 // inside the wall.
 __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float fy, float fz, float m,
                                           float d0f, const double* d0, int g, double (&u)[3],
-                                          double (&v)[3], float (&a)[3], bool& in_contact) {
+                                          double (&v)[3], float (&a)[3], bool& in_contact,
+                                          float (&uf_out)[3], float (&vf_out)[3]) {
   const float rm = __frcp_rn(m);
   a[0] = __fadd_rn(__fmul_rn(-fx, rm), p.gf[0]);
   a[1] = __fadd_rn(__fmul_rn(-fy, rm), p.gf[1]);
@@ -564,19 +571,25 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
   for (int k = 0; k < 3; k++) {
     v[k] = __fma_rn(p.dt, ad[k], v[k]);
     u[k] = un[k];
+    uf_out[k] = uf[k];
+    vf_out[k] = (float)v[k];
   }
 }
 
 __device__ __forceinline__ void store_node(const FusedArgs& A, double* const (&uo)[3],
-                                           double* const (&vo)[3], int g, const double (&u)[3],
-                                           const double (&v)[3], const float (&a)[3],
+                                           double* const (&vo)[3], float* const (&ufo)[3],
+                                           float* const (&vfo)[3], int g, const double (&u)[3],
+                                           const double (&v)[3], const float (&uf)[3],
+                                           const float (&vf)[3], const float (&a)[3],
                                            bool in_contact, bool store_acc) {
   bool finite = true;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     uo[k][g] = u[k];
     vo[k][g] = v[k];
-    finite = finite && isfinite((float)v[k]);
+    ufo[k][g] = uf[k];
+    vfo[k][g] = vf[k];
+    finite = finite && isfinite(vf[k]);
     if (store_acc) A.acc[k][g] = a[k];
   }
   if (!finite) atomicOr(A.status, (unsigned)ST_NONFINITE);
@@ -585,28 +598,42 @@ __device__ __forceinline__ void store_node(const FusedArgs& A, double* const (&u
   if (flag != old) A.contact[g] = flag;
 }
 
+// Shared-memory node records of the fused kernels: p0 = (x, y, z, du_x),
+// p1 = (du_y, du_z), acc = (f_x, f_y, f_z, -); 40 bytes per local node.
+struct Tile {
+  float4* p0;
+  float2* p1;
+  float4* acc;
+};
+
+__device__ __forceinline__ Tile make_tile(float* sm, int L) {
+  Tile t;
+  t.p0 = reinterpret_cast<float4*>(sm);
+  t.p1 = reinterpret_cast<float2*>(t.p0 + L);
+  t.acc = reinterpret_cast<float4*>(t.p1 + ((L + 1) & ~1));
+  return t;
+}
+
 // Stage S^n of every local node of the chunk in shared memory (x relative to the
 // chunk origin, dt v), bringing boundary nodes from S^{n-1} to S^n first.
 template <int BS>
 __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams& ep,
                                             const NodeParams& np, const ChunkInfo& ch,
-                                            int bnd_final, float* sx, float* sd, float* sa) {
+                                            int bnd_final, const Tile& T) {
   const DevPlan& P = A.P;
   const int L = ch.n_local;
-  // interior nodes: contiguous owned range, independent loads (unrolled for MLP)
+  // interior nodes: contiguous owned range, FP32 copies, independent loads
   const int n_direct = bnd_final ? L : ch.n_int;
 #pragma unroll 4
   for (int l = threadIdx.x; l < n_direct; l += BS) {
     const int lb = ch.local_begin + l;
     const int g = l < ch.n_int ? ch.own_begin + l : P.local_gid[lb];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      const double u = A.u_cur[k][g];
-      const double v = A.v_cur[k][g];
-      sx[k * L + l] = P.local_x0[(size_t)k * P.Lt + lb] + (float)u;
-      sd[k * L + l] = ep.dt * (float)v;
-      sa[k * L + l] = 0.f;
-    }
+    const float ux = A.uf_cur[0][g], uy = A.uf_cur[1][g], uz = A.uf_cur[2][g];
+    const float vx = A.vf_cur[0][g], vy = A.vf_cur[1][g], vz = A.vf_cur[2][g];
+    T.p0[l] = make_float4(P.local_x0[lb] + ux, P.local_x0[(size_t)P.Lt + lb] + uy,
+                          P.local_x0[2 * (size_t)P.Lt + lb] + uz, ep.dt * vx);
+    T.p1[l] = make_float2(ep.dt * vy, ep.dt * vz);
+    T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   // boundary nodes: sum the previous step's partial forces and apply the update
 #pragma unroll 2
@@ -626,44 +653,44 @@ __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams
       u[k] = A.u_prv[k][g];
       v[k] = A.v_prv[k][g];
     }
-    float a[3];
+    float a[3], uf[3], vf[3];
     bool hit;
-    node_step(np, fx, fy, fz, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit);
-    if (l < ch.n_own) store_node(A, A.u_cur, A.v_cur, g, u, v, a, hit, false);
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      sx[k * L + l] = P.local_x0[(size_t)k * P.Lt + lb] + (float)u[k];
-      sd[k * L + l] = ep.dt * (float)v[k];
-      sa[k * L + l] = 0.f;
-    }
+    node_step(np, fx, fy, fz, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit, uf, vf);
+    if (l < ch.n_own) store_node(A, A.u_cur, A.v_cur, A.uf_cur, A.vf_cur, g, u, v, uf, vf, a, hit, false);
+    T.p0[l] = make_float4(P.local_x0[lb] + uf[0], P.local_x0[(size_t)P.Lt + lb] + uf[1],
+                          P.local_x0[2 * (size_t)P.Lt + lb] + uf[2], ep.dt * vf[0]);
+    T.p1[l] = make_float2(ep.dt * vf[1], ep.dt * vf[2]);
+    T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 
 // Interior nodes S^n -> S^{n+1} (other buffer); boundary partial forces to the halo.
 template <int BS>
 __device__ __forceinline__ void node_epilogue(const FusedArgs& A, const NodeParams& np,
-                                              const ChunkInfo& ch, const float* sa) {
+                                              const ChunkInfo& ch, const Tile& T) {
   const DevPlan& P = A.P;
   const int L = ch.n_local;
 #pragma unroll 2
   for (int l = threadIdx.x; l < L; l += BS) {
+    const float4 f = T.acc[l];
     if (l < ch.n_int) {
       const int g = ch.own_begin + l;
       double u[3], v[3];
-      float a[3];
+      float a[3], uf[3], vf[3];
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         u[k] = A.u_cur[k][g];
         v[k] = A.v_cur[k][g];
       }
       bool hit;
-      node_step(np, sa[l], sa[L + l], sa[2 * L + l], A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit);
-      store_node(A, A.u_prv, A.v_prv, g, u, v, a, hit, A.store_acc != 0);
+      node_step(np, f.x, f.y, f.z, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit, uf, vf);
+      store_node(A, A.u_prv, A.v_prv, A.uf_prv, A.vf_prv, g, u, v, uf, vf, a, hit,
+                 A.store_acc != 0);
     } else {
       const int s = P.local_slot[ch.local_begin + l];
-      A.halo_cur[0][s] = sa[l];
-      A.halo_cur[1][s] = sa[L + l];
-      A.halo_cur[2][s] = sa[2 * L + l];
+      A.halo_cur[0][s] = f.x;
+      A.halo_cur[1][s] = f.y;
+      A.halo_cur[2][s] = f.z;
     }
   }
 }
@@ -690,12 +717,10 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, Nod
   const ElemParams& ep = cs.ep;
   const NodeParams& np = cs.np;
   const int L = ch.n_local;
-  float* sx = sm;
-  float* sd = sm + 3 * L;
-  float* sa = sm + 6 * L;
+  const Tile T = make_tile(sm, L);
   __shared__ float red[BS / 32];
 
-  stage_nodes<BS>(A, ep, np, ch, cs.bnd_final, sx, sd, sa);
+  stage_nodes<BS>(A, ep, np, ch, cs.bnd_final, T);
   if (cs.mode == 1) return;
   __syncthreads();
 
@@ -718,11 +743,14 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, Nod
 #pragma unroll
       for (int a = 0; a < NPE; a++) {
         ln[a] = P.conn_local[(size_t)a * E + e];
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          x[a][k] = sx[k * L + ln[a]];
-          du[a][k] = sd[k * L + ln[a]];
-        }
+        const float4 q0 = T.p0[ln[a]];
+        const float2 q1 = T.p1[ln[a]];
+        x[a][0] = q0.x;
+        x[a][1] = q0.y;
+        x[a][2] = q0.z;
+        du[a][0] = q0.w;
+        du[a][1] = q1.x;
+        du[a][2] = q1.y;
       }
       element_force<NPE, MODE>(ep, S, e, E, x, du, f, wint, wp, vol);
     }
@@ -733,15 +761,17 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, Nod
       if (col == k) {
 #pragma unroll
         for (int a = 0; a < NPE; a++) {
-          sa[ln[a]] += f[a][0];
-          sa[L + ln[a]] += f[a][1];
-          sa[2 * L + ln[a]] += f[a][2];
+          float4 t = T.acc[ln[a]];
+          t.x += f[a][0];
+          t.y += f[a][1];
+          t.z += f[a][2];
+          T.acc[ln[a]] = t;
         }
       }
     }
   }
   __syncthreads();
-  node_epilogue<BS>(A, np, ch, sa);
+  node_epilogue<BS>(A, np, ch, T);
   if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
 }
 
@@ -805,16 +835,19 @@ __device__ __forceinline__ float tet10_force(const Tet10QP& t, const float* Pa) 
 }
 
 template <int I>
-__device__ __forceinline__ void tet10_gather(const Tet10QP& t, const float* sx, const float* sd,
-                                             int L, int l, float (&J)[9], float (&Gu)[9]) {
+__device__ __forceinline__ void tet10_gather(const Tet10QP& t, const Tile& T, int l, float (&J)[9],
+                                             float (&Gu)[9]) {
+  const float4 q0 = T.p0[l];
+  const float2 q1 = T.p1[l];
+  const float xs[3] = {q0.x, q0.y, q0.z}, ds[3] = {q0.w, q1.x, q1.y};
   float cj[3], cu[3];
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     cj[0] = J[3 * a]; cj[1] = J[3 * a + 1]; cj[2] = J[3 * a + 2];
-    tet10_grad_acc<I>(t, sx[a * L + l], cj);
+    tet10_grad_acc<I>(t, xs[a], cj);
     J[3 * a] = cj[0]; J[3 * a + 1] = cj[1]; J[3 * a + 2] = cj[2];
     cu[0] = Gu[3 * a]; cu[1] = Gu[3 * a + 1]; cu[2] = Gu[3 * a + 2];
-    tet10_grad_acc<I>(t, sd[a * L + l], cu);
+    tet10_grad_acc<I>(t, ds[a], cu);
     Gu[3 * a] = cu[0]; Gu[3 * a + 1] = cu[1]; Gu[3 * a + 2] = cu[2];
   }
 }
@@ -846,12 +879,10 @@ __global__ void __launch_bounds__(BS) k_step_qp10(FusedArgs A, ElemParams ep_arg
   const ElemParams& ep = cs.ep;
   const NodeParams& np = cs.np;
   const int L = ch.n_local;
-  float* sx = sm;
-  float* sd = sm + 3 * L;
-  float* sa = sm + 6 * L;
+  const Tile T = make_tile(sm, L);
   __shared__ float red[BS / 32];
 
-  stage_nodes<BS>(A, ep, np, ch, cs.bnd_final, sx, sd, sa);
+  stage_nodes<BS>(A, ep, np, ch, cs.bnd_final, T);
   if (cs.mode == 1) return;
   __syncthreads();
 
@@ -880,16 +911,16 @@ __global__ void __launch_bounds__(BS) k_step_qp10(FusedArgs A, ElemParams ep_arg
     float J[9], Gu[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) J[k] = Gu[k] = 0.f;
-    tet10_gather<0>(t, sx, sd, L, ln[0], J, Gu);
-    tet10_gather<1>(t, sx, sd, L, ln[1], J, Gu);
-    tet10_gather<2>(t, sx, sd, L, ln[2], J, Gu);
-    tet10_gather<3>(t, sx, sd, L, ln[3], J, Gu);
-    tet10_gather<4>(t, sx, sd, L, ln[4], J, Gu);
-    tet10_gather<5>(t, sx, sd, L, ln[5], J, Gu);
-    tet10_gather<6>(t, sx, sd, L, ln[6], J, Gu);
-    tet10_gather<7>(t, sx, sd, L, ln[7], J, Gu);
-    tet10_gather<8>(t, sx, sd, L, ln[8], J, Gu);
-    tet10_gather<9>(t, sx, sd, L, ln[9], J, Gu);
+    tet10_gather<0>(t, T, ln[0], J, Gu);
+    tet10_gather<1>(t, T, ln[1], J, Gu);
+    tet10_gather<2>(t, T, ln[2], J, Gu);
+    tet10_gather<3>(t, T, ln[3], J, Gu);
+    tet10_gather<4>(t, T, ln[4], J, Gu);
+    tet10_gather<5>(t, T, ln[5], J, Gu);
+    tet10_gather<6>(t, T, ln[6], J, Gu);
+    tet10_gather<7>(t, T, ln[7], J, Gu);
+    tet10_gather<8>(t, T, ln[8], J, Gu);
+    tet10_gather<9>(t, T, ln[9], J, Gu);
     float Ji[9];
     const float detJ = inv3f(J, Ji);
     if (act && !(detJ > 0.f)) atomicOr(A.status, (unsigned)ST_DEGENERATE);
@@ -956,22 +987,28 @@ __global__ void __launch_bounds__(BS) k_step_qp10(FusedArgs A, ElemParams ep_arg
     for (int k = c0; k <= c1; k++) {
       __syncthreads();
       if (col == k) {
-        sa[own0] += keep[0][0];
-        sa[L + own0] += keep[0][1];
-        sa[2 * L + own0] += keep[0][2];
-        sa[own1] += keep[1][0];
-        sa[L + own1] += keep[1][1];
-        sa[2 * L + own1] += keep[1][2];
+        float4 t0 = T.acc[own0];
+        t0.x += keep[0][0];
+        t0.y += keep[0][1];
+        t0.z += keep[0][2];
+        T.acc[own0] = t0;
+        float4 t1 = T.acc[own1];
+        t1.x += keep[1][0];
+        t1.y += keep[1][1];
+        t1.z += keep[1][2];
+        T.acc[own1] = t1;
         if (q < 2) {
-          sa[own2] += keep[2][0];
-          sa[L + own2] += keep[2][1];
-          sa[2 * L + own2] += keep[2][2];
+          float4 t2 = T.acc[own2];
+          t2.x += keep[2][0];
+          t2.y += keep[2][1];
+          t2.z += keep[2][2];
+          T.acc[own2] = t2;
         }
       }
     }
   }
   __syncthreads();
-  node_epilogue<BS>(A, np, ch, sa);
+  node_epilogue<BS>(A, np, ch, T);
   if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
 }
 
@@ -990,15 +1027,15 @@ static __global__ void __launch_bounds__(256) k_finalize_boundary(FusedArgs A, N
     fz = __fadd_rn(fz, A.halo_prv[2][s]);
   }
   double u[3], v[3];
-  float a[3];
+  float a[3], uf[3], vf[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     u[k] = A.u_prv[k][g];
     v[k] = A.v_prv[k][g];
   }
   bool hit;
-  node_step(np, fx, fy, fz, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit);
-  store_node(A, A.u_cur, A.v_cur, g, u, v, a, hit, true);
+  node_step(np, fx, fy, fz, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit, uf, vf);
+  store_node(A, A.u_cur, A.v_cur, A.uf_cur, A.vf_cur, g, u, v, uf, vf, a, hit, true);
 }
 
 // a0 from zero internal force (wall at the start positions, gravity) and the half step
@@ -1043,6 +1080,14 @@ __global__ void __launch_bounds__(256) k_node_init(NodeArrays A, NodeParams p_ar
   }
   A.contact[n] = flag;
   if (!finite) atomicOr(A.status, (unsigned)ST_NONFINITE);
+}
+
+// FP32 copies of the FP64 state (after it was written by an initial condition).
+static __global__ void k_shadows(const double* u, const double* v, float* uf, float* vf, long long n3) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  uf[i] = (float)u[i];
+  vf[i] = (float)v[i];
 }
 
 // Adds n to the batched step counter (after each captured block of steps).

@@ -97,6 +97,7 @@ struct ci_solver {
   // path's second buffer)
   DBuf<double> d_u, d_v;   // [3][N]
   DBuf<double> d_ub, d_vb; // [3][N]
+  DBuf<float> d_ufa, d_vfa, d_ufb, d_vfb;  // FP32 copies of u, v (A and B buffers)
   DBuf<float> d_halo1;     // [3][S] second halo buffer of the fused path
   DBuf<int> d_bnd;         // boundary nodes (plan ids)
   int n_bnd = 0;
@@ -190,6 +191,10 @@ struct ci_solver {
       F.v_cur[k] = (cur_is_a ? va : vb) + (size_t)k * N;
       F.u_prv[k] = (cur_is_a ? ub : ua) + (size_t)k * N;
       F.v_prv[k] = (cur_is_a ? vb : va) + (size_t)k * N;
+      F.uf_cur[k] = (cur_is_a ? d_ufa.p : d_ufb.p) + (size_t)k * N;
+      F.vf_cur[k] = (cur_is_a ? d_vfa.p : d_vfb.p) + (size_t)k * N;
+      F.uf_prv[k] = (cur_is_a ? d_ufb.p : d_ufa.p) + (size_t)k * N;
+      F.vf_prv[k] = (cur_is_a ? d_vfb.p : d_vfa.p) + (size_t)k * N;
       F.halo_cur[k] = h[halo_cur] + (size_t)k * S;
       F.halo_prv[k] = h[halo_cur ^ 1] + (size_t)k * S;
       F.acc[k] = d_acc.p + (size_t)k * N;
@@ -323,9 +328,11 @@ cudaError_t enqueue_fused(ci_solver* s, int n, bool store_acc_last) {
   const ci::FusedArgs F = s->fused_args((n & 1) == 0, n & 1, false, true);
   if ((e = launch_finalize(s, F))) return e;
   if (n & 1) {
-    const size_t b = sizeof(double) * 3 * (size_t)s->N;
+    const size_t b = sizeof(double) * 3 * (size_t)s->N, bf = sizeof(float) * 3 * (size_t)s->N;
     if ((e = cudaMemcpyAsync(s->d_u.p, s->d_ub.p, b, cudaMemcpyDeviceToDevice, s->stream))) return e;
     if ((e = cudaMemcpyAsync(s->d_v.p, s->d_vb.p, b, cudaMemcpyDeviceToDevice, s->stream))) return e;
+    if ((e = cudaMemcpyAsync(s->d_ufa.p, s->d_ufb.p, bf, cudaMemcpyDeviceToDevice, s->stream))) return e;
+    if ((e = cudaMemcpyAsync(s->d_vfa.p, s->d_vfb.p, bf, cudaMemcpyDeviceToDevice, s->stream))) return e;
   }
   return cudaSuccess;
 }
@@ -361,6 +368,15 @@ cudaError_t enqueue_step(ci_solver* s, bool store_acc) {
     ci::k_node<false, true><<<nb, 256, 0, s->stream>>>(s->node_arrays(), s->node_params());
   else
     ci::k_node<false, false><<<nb, 256, 0, s->stream>>>(s->node_arrays(), s->node_params());
+  return cudaGetLastError();
+}
+
+// FP32 copies of the A-buffer state (fused path), after the FP64 state was written.
+cudaError_t refresh_shadows(ci_solver* s) {
+  if (!s->d_ufa.p) return cudaSuccess;
+  const long long n3 = 3 * (long long)s->N;
+  ci::k_shadows<<<(unsigned)((n3 + 255) / 256), 256, 0, s->stream>>>(s->d_u.p, s->d_v.p, s->d_ufa.p,
+                                                                   s->d_vfa.p, n3);
   return cudaGetLastError();
 }
 
@@ -590,7 +606,8 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   s->C = P.n_chunks;
   s->S = P.slot_row[s->N];
   s->Lt = (long long)P.local_gid.size();
-  s->smem_bytes = sizeof(float) * 9 * (size_t)P.max_local;
+  // fused kernels: 40 B per local node (+ alignment); the element kernel: 36 B
+  s->smem_bytes = 40 * ((size_t)P.max_local + 2);
   int smem_max = 0;
   CI_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
   if ((long long)s->smem_bytes + 1024 > smem_max)
@@ -618,6 +635,10 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   if (s->opt.step_kernel == 0) {
     CI_CUDA(s->d_ub.alloc(3 * N));
     CI_CUDA(s->d_vb.alloc(3 * N));
+    CI_CUDA(s->d_ufa.alloc(3 * N));
+    CI_CUDA(s->d_vfa.alloc(3 * N));
+    CI_CUDA(s->d_ufb.alloc(3 * N));
+    CI_CUDA(s->d_vfb.alloc(3 * N));
     CI_CUDA(s->d_halo1.alloc(3 * (size_t)s->S));
     std::vector<int> bnd;
     for (int n = 0; n < s->N; n++)
@@ -678,6 +699,7 @@ int ci_start(ci_solver* s, double dt) {
   ci::k_node_init<false><<<(s->N + 255) / 256, 256, 0, s->stream>>>(
       s->node_arrays(), s->node_params(), nullptr, nullptr, s->d_d0f.p);
   CI_CUDA(cudaGetLastError());
+  CI_CUDA(refresh_shadows(s));
   s->started = true;
   return check_status(s);
 }
@@ -795,6 +817,7 @@ int ci_set_state(ci_solver* s, const double* x, const double* v) {
                           s->stream));
   CI_CUDA(cudaMemcpyAsync(s->d_v.p, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice,
                           s->stream));
+  CI_CUDA(refresh_shadows(s));
   CI_CUDA(cudaStreamSynchronize(s->stream));
   return CI_OK;
 }
@@ -1028,9 +1051,11 @@ int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms) {
     CI_CUDA(launch_finalize(s, F));
     CI_CUDA(cudaEventRecord(ev[2], s->stream));
     if (nsteps & 1) {
-      const size_t b = sizeof(double) * 3 * (size_t)s->N;
+      const size_t b = sizeof(double) * 3 * (size_t)s->N, bf = sizeof(float) * 3 * (size_t)s->N;
       CI_CUDA(cudaMemcpyAsync(s->d_u.p, s->d_ub.p, b, cudaMemcpyDeviceToDevice, s->stream));
       CI_CUDA(cudaMemcpyAsync(s->d_v.p, s->d_vb.p, b, cudaMemcpyDeviceToDevice, s->stream));
+      CI_CUDA(cudaMemcpyAsync(s->d_ufa.p, s->d_ufb.p, bf, cudaMemcpyDeviceToDevice, s->stream));
+      CI_CUDA(cudaMemcpyAsync(s->d_vfa.p, s->d_vfb.p, bf, cudaMemcpyDeviceToDevice, s->stream));
     }
     CI_CUDA(cudaStreamSynchronize(s->stream));
     for (int i = 0; i < nsteps; i++) {

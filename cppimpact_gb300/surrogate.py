@@ -1,0 +1,314 @@
+"""Learned surrogate for parameter sweeps: POD basis of displacement snapshots + MLP.
+
+Pipeline (all dense algebra on the GPU through the library's BF16 tcgen05 GEMM and
+MLP entry points; PyTorch only holds device buffers):
+
+1. ``generate``: seeded impact parameters (velocity, yield stress, hardening, wall
+   tilt) -> one batched solve of the tet4 cube per parameter set, with the
+   displacement of every node recorded every ``every`` steps (``ci_batch_run_snapshots``).
+2. ``pod``: rank-r POD basis of all training snapshots by a randomized range finder
+   (Halko, Martinsson & Tropp 2011): Y = S Omega, Q = orth(Y), W = S^T Q, then the small
+   eigenproblem of W^T W by cyclic Jacobi rotations in FP64 on the host.
+3. modal trajectories A = S Phi; an MLP (4 -> H -> H -> r*snaps) maps normalised
+   parameters to normalised modal trajectories, trained with ``ci_mlp_train``.
+4. ``predict``: ensemble mean of several MLPs, reconstruction u = A Phi^T, peak
+   displacement; queries whose ensemble spread exceeds the threshold, and an audited
+   random fraction, are re-run by the plain solver (``fallback``).
+The method without the network, for comparison, interpolates the training runs'
+modal trajectories by inverse-distance weighting in parameter space.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+import time
+
+import numpy as np
+
+from . import api
+from . import meshgen as mg
+from .sweep import tilted_setup
+
+E, NU, RHO = 68.9e9, 0.33, 2700.0
+LO = np.array([2.0, 200e6, 0.005, 0.0])   # velocity, yield, hardening / E, tilt (deg)
+HI = np.array([20.0, 350e6, 0.02, 15.0])
+
+
+@dataclasses.dataclass
+class Config:
+    n_cube: int = 12
+    steps: int = 4000
+    every: int = 50
+    rank: int = 64
+    hidden: int = 256
+    n_train: int = 4096
+    n_test: int = 512
+    epochs: int = 300
+    batch: int = 256
+    lr: float = 2e-3
+    ensemble: int = 3
+    spread_threshold: float = 0.01
+    audit_fraction: float = 0.05
+    error_threshold: float = 0.02
+    seed: int = mg.DEFAULT_SEED
+
+    @property
+    def snaps(self) -> int:
+        return self.steps // self.every
+
+
+def sample_params(n: int, rng) -> np.ndarray:
+    return LO + (HI - LO) * rng.random((n, 4))
+
+
+def normalise(p: np.ndarray) -> np.ndarray:
+    return (2.0 * (p - LO) / (HI - LO) - 1.0).astype(np.float32)
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream(torch):
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def gemm(A, B, transA=False, transB=False, out=None, out_bf16=None, beta=0.0):
+    """C = op(A) op(B) with the library's BF16 tensor-core GEMM (torch CUDA tensors)."""
+    torch = _torch()
+    assert A.dtype == torch.bfloat16 and B.dtype == torch.bfloat16
+    M = A.shape[1] if transA else A.shape[0]
+    K = A.shape[0] if transA else A.shape[1]
+    N = B.shape[0] if transB else B.shape[1]
+    if out is None:
+        out = torch.zeros((M, N), dtype=torch.float32, device=A.device)
+    err = torch.zeros(1, dtype=torch.int32, device=A.device)
+    api.check(api.lib().ci_gemm_bf16(A.data_ptr(), A.shape[1], int(transA), B.data_ptr(), B.shape[1],
+                                     int(transB), out.data_ptr(), out.shape[1],
+                                     None if out_bf16 is None else out_bf16.data_ptr(), M, N, K,
+                                     1.0, beta, None, 0, err.data_ptr(), _stream(torch)))
+    if int(err.item()) != 0:
+        raise RuntimeError("tensor-core GEMM timed out")
+    return out
+
+
+def jacobi_eigh(A: np.ndarray, sweeps: int = 60, tol: float = 1e-14):
+    """Eigen-decomposition of a small symmetric matrix by cyclic Jacobi rotations
+    (Golub & Van Loan, Matrix Computations, 4th ed., section 8.5); descending order."""
+    A = np.array(A, dtype=np.float64, copy=True)
+    n = A.shape[0]
+    V = np.eye(n)
+    for _ in range(sweeps):
+        off = np.sqrt(np.sum(np.tril(A, -1) ** 2))
+        if off <= tol * np.sqrt(np.sum(A * A)):
+            break
+        for p in range(n - 1):
+            for q in range(p + 1, n):
+                if abs(A[p, q]) < 1e-300:
+                    continue
+                tau = (A[q, q] - A[p, p]) / (2.0 * A[p, q])
+                t = math.copysign(1.0, tau) / (abs(tau) + math.sqrt(1.0 + tau * tau))
+                c = 1.0 / math.sqrt(1.0 + t * t)
+                s = t * c
+                Ap, Aq = A[:, p].copy(), A[:, q].copy()
+                A[:, p], A[:, q] = c * Ap - s * Aq, s * Ap + c * Aq
+                Ap, Aq = A[p, :].copy(), A[q, :].copy()
+                A[p, :], A[q, :] = c * Ap - s * Aq, s * Ap + c * Aq
+                Vp, Vq = V[:, p].copy(), V[:, q].copy()
+                V[:, p], V[:, q] = c * Vp - s * Vq, s * Vp + c * Vq
+    w = np.diag(A).copy()
+    order = np.argsort(-w)
+    return w[order], V[:, order]
+
+
+def generate(params: np.ndarray, cfg: Config, mesh: mg.TetMesh | None = None):
+    """Batched solves; returns (snapshots [n, snaps, 3N] FP32 torch in caller node order,
+    peak equivalent plastic strain [n], device ms)."""
+    torch = _torch()
+    mesh = mesh or mg.cube(cfg.n_cube, 1)
+    inst = []
+    for v, sy, h, tilt in params:
+        st = tilted_setup(mesh, v, tilt)
+        st["t_end"] = (cfg.steps - 0.5) * st["dt"]
+        inst.append(dict(xloc=mesh.xloc, conn=mesh.conn, E=E, nu=NU, rho=RHO, sigma_y0=sy,
+                         H=h * E, **st))
+    b = api.Batch(inst)
+    n, N = len(inst), mesh.num_nodes
+    snap = torch.zeros((cfg.snaps, n * N, 3), dtype=torch.float32, device="cuda")
+    ms = b.run_snapshots(cfg.every, snap.data_ptr(), cfg.snaps)
+    perm, _ = b.node_order(0)
+    inv = np.argsort(perm)          # caller node -> plan position
+    s = snap.view(cfg.snaps, n, N, 3)[:, :, torch.as_tensor(inv, device="cuda"), :]
+    s = s.permute(1, 0, 2, 3).reshape(n, cfg.snaps, 3 * N).contiguous()
+    peak_ep = np.array([float(b.state(i)["epbar"].max()) for i in range(n)])
+    b.close()
+    return s, peak_ep, ms
+
+
+def peak_disp(snaps) -> "torch.Tensor":
+    """max over snapshots and nodes of the nodal displacement norm, per run."""
+    n, k, d = snaps.shape
+    return snaps.view(n, k, d // 3, 3).norm(dim=3).amax(dim=(1, 2))
+
+
+def pod(S, rank: int, oversample: int = 32, seed: int = 0):
+    """Rank-r right singular vectors of the snapshot matrix S [rows x dofs] (BF16)."""
+    torch = _torch()
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    k = rank + oversample
+    dofs = S.shape[1]
+    Om = torch.randn((dofs, k), generator=g, device="cuda").to(torch.bfloat16)
+    Yb = torch.empty((S.shape[0], k), dtype=torch.bfloat16, device="cuda")
+    gemm(S, Om, out_bf16=Yb)                               # Y = S Omega
+    G = gemm(Yb, Yb, transA=True).double().cpu().numpy()   # Y^T Y
+    w, U = jacobi_eigh(G)
+    keep = w > w[0] * 1e-10
+    Rinv = U[:, keep] / np.sqrt(w[keep])[None, :]          # Q = Y U diag(w)^-1/2
+    Rb = torch.tensor(Rinv, dtype=torch.float32, device="cuda").to(torch.bfloat16).contiguous()
+    Qb = torch.empty((S.shape[0], Rb.shape[1]), dtype=torch.bfloat16, device="cuda")
+    gemm(Yb, Rb, out_bf16=Qb)
+    W = gemm(S, Qb, transA=True).double().cpu().numpy()    # W = S^T Q  [dofs x k]
+    w2, U2 = jacobi_eigh(W.T @ W)
+    V = W @ U2[:, :rank] / np.sqrt(np.maximum(w2[:rank], 1e-300))[None, :]
+    # orthonormalise (modified Gram-Schmidt, FP64)
+    for j in range(rank):
+        for i in range(j):
+            V[:, j] -= (V[:, i] @ V[:, j]) * V[:, i]
+        V[:, j] /= np.linalg.norm(V[:, j])
+    return V, np.sqrt(np.maximum(w2[:rank], 0.0))
+
+
+class MLP:
+    """Handle on a library MLP (ci_mlp_*)."""
+
+    def __init__(self, n_in, hidden, n_out, seed):
+        self._h = C.c_void_p()
+        api.check(api.lib().ci_mlp_create(n_in, hidden, n_out, seed, C.byref(self._h)))
+        self.n_in, self.n_out = n_in, n_out
+
+    def train(self, X, T, epochs, batch, lr, seed):
+        torch = _torch()
+        loss = np.zeros(epochs)
+        api.check(api.lib().ci_mlp_train(self._h, X.data_ptr(), T.data_ptr(), X.shape[0], batch,
+                                         epochs, lr, seed, loss.ctypes.data_as(C.POINTER(C.c_double)),
+                                         _stream(torch)))
+        torch.cuda.synchronize()
+        return loss
+
+    def predict(self, X):
+        torch = _torch()
+        Y = torch.empty((X.shape[0], self.n_out), dtype=torch.float32, device="cuda")
+        api.check(api.lib().ci_mlp_predict(self._h, X.data_ptr(), X.shape[0], Y.data_ptr(),
+                                           _stream(torch)))
+        return Y
+
+    def gradients(self, X, T):
+        n = api.lib().ci_mlp_num_params(self._h)
+        g = np.zeros(n, dtype=np.float32)
+        loss = C.c_double(0)
+        api.check(api.lib().ci_mlp_gradients(self._h, X.data_ptr(), T.data_ptr(), X.shape[0],
+                                             g.ctypes.data_as(C.POINTER(C.c_float)),
+                                             C.byref(loss)))
+        return g, loss.value
+
+    def params(self):
+        n = api.lib().ci_mlp_num_params(self._h)
+        p = np.zeros(n, dtype=np.float32)
+        api.check(api.lib().ci_mlp_get_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        api.check(api.lib().ci_mlp_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def close(self):
+        if self._h.value:
+            api.lib().ci_mlp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Surrogate:
+    def __init__(self, cfg: Config):
+        self.cfg = cfg
+        self.mesh = mg.cube(cfg.n_cube, 1)
+        self.timings = {}
+
+    def fit(self, params: np.ndarray, snaps):
+        """params [n x 4], snaps [n, snaps, 3N] (torch FP32)."""
+        torch = _torch()
+        cfg = self.cfg
+        n, k, d = snaps.shape
+        t0 = time.perf_counter()
+        S = snaps.reshape(n * k, d).to(torch.bfloat16).contiguous()
+        Phi, sv = pod(S, cfg.rank, seed=cfg.seed)
+        self.Phi = Phi
+        self.Phib = torch.tensor(Phi, dtype=torch.float32, device="cuda").to(torch.bfloat16).contiguous()
+        A = gemm(S, self.Phib)                              # modal trajectories [n*k x r]
+        torch.cuda.synchronize()
+        self.timings["pod_s"] = time.perf_counter() - t0
+        rel = float((S.float() - gemm(A.to(torch.bfloat16).contiguous(), self.Phib, transB=True)).norm()
+                    / S.float().norm())
+        self.pod_error = rel
+        Y = A.view(n, k * cfg.rank)
+        self.y_mean = Y.mean(dim=0, keepdim=True)
+        self.y_std = Y.std(dim=0, keepdim=True) + 1e-12 * Y.abs().max()
+        Yn = ((Y - self.y_mean) / self.y_std).contiguous()
+        X = torch.tensor(normalise(params), device="cuda")
+        self.train_X, self.train_Y = X, Y
+        t0 = time.perf_counter()
+        self.nets, self.losses = [], []
+        for j in range(cfg.ensemble):
+            net = MLP(4, cfg.hidden, k * cfg.rank, cfg.seed + 101 * j)
+            self.losses.append(net.train(X, Yn, cfg.epochs, cfg.batch, cfg.lr, cfg.seed + 7 * j))
+            self.nets.append(net)
+        torch.cuda.synchronize()
+        self.timings["train_s"] = time.perf_counter() - t0
+
+    def _reconstruct_peak(self, A):
+        """A [n, snaps * r] modal trajectories -> peak displacement per run."""
+        torch = _torch()
+        n = A.shape[0]
+        k, r = self.cfg.snaps, self.cfg.rank
+        U = gemm(A.view(n * k, r).to(torch.bfloat16).contiguous(), self.Phib, transB=True)
+        return peak_disp(U.view(n, k, -1))
+
+    def predict(self, params: np.ndarray):
+        """Ensemble prediction: (peak displacement mean, relative spread) per query."""
+        torch = _torch()
+        X = torch.tensor(normalise(params), device="cuda")
+        peaks = []
+        for net in self.nets:
+            A = net.predict(X) * self.y_std + self.y_mean
+            peaks.append(self._reconstruct_peak(A))
+        P = torch.stack(peaks)
+        mean = P.mean(dim=0)
+        spread = P.std(dim=0) / mean.clamp_min(1e-30) if len(peaks) > 1 else torch.zeros_like(mean)
+        return mean, spread
+
+    def predict_idw(self, params: np.ndarray, k_nn: int = 8):
+        """The method without the network: inverse-distance-weighted interpolation of the
+        training runs' modal trajectories in normalised parameter space."""
+        torch = _torch()
+        X = torch.tensor(normalise(params), device="cuda")
+        d = torch.cdist(X, self.train_X)
+        dist, idx = d.topk(k_nn, largest=False)
+        w = 1.0 / dist.clamp_min(1e-6) ** 2
+        w = w / w.sum(dim=1, keepdim=True)
+        A = (self.train_Y[idx] * w[..., None]).sum(dim=1)
+        return self._reconstruct_peak(A)
+
+
+def fallback_runs(params: np.ndarray, cfg: Config, mesh=None):
+    """Plain solver for the given queries (one batch); peak displacement, device ms."""
+    if len(params) == 0:
+        return np.zeros(0), 0.0
+    s, _, ms = generate(params, cfg, mesh)
+    return peak_disp(s).cpu().numpy(), ms

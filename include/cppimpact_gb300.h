@@ -194,6 +194,49 @@ int ci_batch_run(ci_batch* b, float* device_ms);
 int ci_batch_get_state(ci_batch* b, int i, double* x, double* v, float* epbar,
                        unsigned char* contact, long long* nsteps);
 int ci_batch_destroy(ci_batch* b);
+/* A run of a batch of one element type that also records the displacement of every
+ * node every `every` steps (even) into d_snap [max_snaps][N_total][3] (device FP32,
+ * plan order, instances concatenated); snapshot s is the state after (s+1)*every
+ * steps.  ci_batch_node_order gives instance i's plan order (perm[p] = caller node)
+ * and its offset in N_total. */
+int ci_batch_run_snapshots(ci_batch* b, int every, float* d_snap, int max_snaps, float* device_ms);
+int ci_batch_node_order(ci_batch* b, int i, int* perm, int* node_offset);
+
+/* ---- BF16 tensor-core GEMM (surrogate training and inference; no reference
+ * counterpart: the reference has no dense contraction) ----
+ * C[M x N] = alpha op(A) op(B) + beta C (+ bias[N]) (then tanh if activation == 1) on
+ * `stream`.  A, B: BF16 row-major with leading dimensions lda, ldb, transA / transB
+ * select op() = transpose.  C: FP32 row-major (ldc); C_bf16 (may be NULL) receives a
+ * BF16 copy.  All pointers are device pointers.  *d_error (device int) is set to 1 if
+ * a tensor-core wait timed out (the result is then invalid).  When the output has few
+ * 128-row tiles and K is long, K is split across CTAs: partial tiles go to a per-device
+ * FP32 workspace (grown by cudaMalloc on first need) and are summed in a fixed order, so
+ * results are deterministic; concurrent calls on different streams of one device must
+ * not overlap. */
+int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, int ldb, int transB, float* C,
+                 int ldc, void* C_bf16, int M, int N, int K, float alpha, float beta,
+                 const float* bias, int activation, int* d_error, void* stream);
+
+/* ---- surrogate MLP (no reference counterpart) ----
+ * n_in -> H -> H -> n_out with tanh hidden layers; every product is ci_gemm_bf16 (BF16
+ * operands, FP32 accumulation); FP32 master weights; Adam.  Parameter order:
+ * W1 [n_in x H], b1 [H], W2 [H x H], b2 [H], W3 [H x n_out], b3 [n_out] (row-major,
+ * a layer computes X W + b).  Data pointers (d_*) are device FP32 row-major. */
+typedef struct ci_mlp ci_mlp;
+int ci_mlp_create(int n_in, int n_hidden, int n_out, unsigned long long seed, ci_mlp** out);
+int ci_mlp_destroy(ci_mlp* m);
+long long ci_mlp_num_params(const ci_mlp* m);
+int ci_mlp_set_params(ci_mlp* m, const float* h_params);
+int ci_mlp_get_params(ci_mlp* m, float* h_params);
+/* d_Y [n x n_out] = MLP(d_X [n x n_in]) */
+int ci_mlp_predict(ci_mlp* m, const float* d_X, int n, float* d_Y, void* stream);
+/* gradients of the mean squared error over all n rows into h_grad [num_params] (host) */
+int ci_mlp_gradients(ci_mlp* m, const float* d_X, const float* d_T, int n, float* h_grad,
+                     double* loss);
+/* epochs of mini-batch Adam (seeded shuffles); h_loss [epochs] (may be NULL) receives the
+ * last mini-batch loss of each epoch */
+int ci_mlp_train(ci_mlp* m, const float* d_X, const float* d_T, int n, int batch, int epochs,
+                 float lr, unsigned long long seed, double* h_loss, void* stream);
 
 /* ---- allocation-free variant (no counterpart in the reference) ----
  * ci_strain_energy_noalloc computes what ci_strain_energy computes -- the total strain

@@ -1,0 +1,80 @@
+"""The BF16 tcgen05 GEMM of the surrogate against a float64 product of the same
+BF16-rounded operands (FP32 accumulation: relative error <= 1e-3 here)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _gemm(cilib, torch, A, B, transA, transB, bias=None, act=0, beta=0.0, C0=None):
+    dev = torch.device("cuda:0")
+    a = torch.tensor(A, dtype=torch.float32, device=dev).to(torch.bfloat16).contiguous()
+    b = torch.tensor(B, dtype=torch.float32, device=dev).to(torch.bfloat16).contiguous()
+    M = A.shape[1] if transA else A.shape[0]
+    K = A.shape[0] if transA else A.shape[1]
+    N = B.shape[0] if transB else B.shape[1]
+    c = (torch.zeros((M, N), dtype=torch.float32, device=dev) if C0 is None
+         else torch.tensor(C0, dtype=torch.float32, device=dev))
+    cb = torch.zeros((M, N), dtype=torch.bfloat16, device=dev)
+    bb = None if bias is None else torch.tensor(bias, dtype=torch.float32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    rc = cilib.lib().ci_gemm_bf16(a.data_ptr(), A.shape[1], transA, b.data_ptr(), B.shape[1],
+                                  transB, c.data_ptr(), N, cb.data_ptr(), M, N, K, 1.0, beta,
+                                  None if bb is None else bb.data_ptr(), act, err.data_ptr(),
+                                  C.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    assert rc == 0, cilib.lib().ci_last_error()
+    torch.cuda.synchronize(dev)
+    assert int(err.item()) == 0
+    Ar = a.float().cpu().numpy().astype(np.float64)
+    Br = b.float().cpu().numpy().astype(np.float64)
+    ref = (Ar.T if transA else Ar) @ (Br.T if transB else Br)
+    if C0 is not None:
+        ref = ref + beta * C0
+    if bias is not None:
+        ref = ref + bias[None, :]
+    if act == 1:
+        ref = np.tanh(ref)
+    return c.cpu().numpy(), ref, cb.float().cpu().numpy()
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (128, 128, 128), (200, 100, 130), (64, 300, 40),
+                                   (1000, 96, 700)])
+@pytest.mark.parametrize("tA,tB", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_gemm_bf16(cilib, M, N, K, tA, tB):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(M * 7 + N * 3 + K + 10 * tA + 20 * tB)
+    A = rng.standard_normal((K, M) if tA else (M, K))
+    B = rng.standard_normal((N, K) if tB else (K, N))
+    c, ref, _ = _gemm(cilib, torch, A, B, tA, tB)
+    assert np.linalg.norm(c - ref) <= 1e-3 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("M,N,K", [(64, 64, 20000), (130, 5, 9000), (8, 200, 4096)])
+@pytest.mark.parametrize("tA,tB", [(1, 0), (0, 1)])
+def test_gemm_bf16_split_k(cilib, M, N, K, tA, tB):
+    """Few output tiles and a long K (the POD's Gram and projection products): the
+    split-K path with its fixed-order reduction; two calls give identical bits."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(M + N + K + tA)
+    A = rng.standard_normal((K, M) if tA else (M, K))
+    B = rng.standard_normal((N, K) if tB else (K, N))
+    bias = rng.standard_normal(N)
+    c, ref, _ = _gemm(cilib, torch, A, B, tA, tB, bias=bias)
+    assert np.linalg.norm(c - ref) <= 1e-3 * np.linalg.norm(ref)
+    c2, _, _ = _gemm(cilib, torch, A, B, tA, tB, bias=bias)
+    assert np.array_equal(c, c2)
+
+
+def test_gemm_bias_tanh_beta(cilib):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(5)
+    A, B = rng.standard_normal((300, 40)) * 0.2, rng.standard_normal((40, 256)) * 0.2
+    bias = rng.standard_normal(256) * 0.1
+    c, ref, cb = _gemm(cilib, torch, A, B, 0, 0, bias=bias, act=1)
+    assert np.abs(c - ref).max() < 2e-3
+    assert np.abs(cb - c).max() < 1e-2
+    C0 = rng.standard_normal((300, 256))
+    c, ref, _ = _gemm(cilib, torch, A, B, 0, 0, beta=0.5, C0=C0)
+    assert np.linalg.norm(c - ref) <= 1e-3 * np.linalg.norm(ref)

@@ -1,0 +1,113 @@
+"""Surrogate pieces on the GPU: MLP gradients against the float64 oracle, POD of a
+known low-rank matrix, snapshots against the batch's own final state, and a small
+end-to-end fit."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mlp_gradients_match_fp64_oracle(cilib):
+    torch = pytest.importorskip("torch")
+    import mlp_oracle
+    from cppimpact_gb300 import surrogate as sg
+    n_in, H, n_out, n = 4, 32, 40, 96
+    rng = np.random.default_rng(3)
+    X = rng.uniform(-1, 1, (n, n_in)).astype(np.float32)
+    T = rng.standard_normal((n, n_out)).astype(np.float32)
+    net = sg.MLP(n_in, H, n_out, seed=5)
+    p = net.params()
+    g, loss = net.gradients(torch.tensor(X, device="cuda"), torch.tensor(T, device="cuda"))
+    # the GPU multiplies BF16-rounded operands: give the oracle the same weights
+    pb = torch.tensor(p).to(torch.bfloat16).float().numpy()
+    loss_ref, g_ref = mlp_oracle.loss_and_grad(pb, X, T, n_in, H, n_out)
+    assert loss == pytest.approx(loss_ref, rel=2e-2)
+    assert np.linalg.norm(g - g_ref) <= 3e-2 * np.linalg.norm(g_ref)
+    # and the direction is right per layer block
+    o = 0
+    for size in (n_in * H, H, H * H, H, H * n_out, n_out):
+        a, b = g[o:o + size], g_ref[o:o + size]
+        assert a @ b > 0.98 * np.linalg.norm(a) * np.linalg.norm(b)
+        o += size
+
+
+def test_mlp_training_reduces_loss(cilib):
+    torch = pytest.importorskip("torch")
+    from cppimpact_gb300 import surrogate as sg
+    rng = np.random.default_rng(1)
+    X = rng.uniform(-1, 1, (512, 4)).astype(np.float32)
+    W = rng.standard_normal((4, 20))
+    T = np.tanh(X @ W).astype(np.float32)
+    net = sg.MLP(4, 64, 20, seed=2)
+    loss = net.train(torch.tensor(X, device="cuda"), torch.tensor(T, device="cuda"), epochs=60,
+                     batch=64, lr=3e-3, seed=4)
+    assert loss[-1] < 0.05 * loss[0]
+
+
+def test_pod_recovers_low_rank_subspace(cilib):
+    torch = pytest.importorskip("torch")
+    from cppimpact_gb300 import surrogate as sg
+    rng = np.random.default_rng(0)
+    rows, dofs, r = 3000, 500, 6
+    V = np.linalg.qr(rng.standard_normal((dofs, r)))[0]
+    S = (rng.standard_normal((rows, r)) * np.array([10, 7, 5, 3, 2, 1.5])) @ V.T
+    S += 1e-3 * rng.standard_normal(S.shape)
+    Phi, sv = sg.pod(torch.tensor(S, dtype=torch.float32, device="cuda").to(torch.bfloat16), r)
+    # principal angles between span(Phi) and span(V)
+    s = np.linalg.svd(Phi.T @ V, compute_uv=False)
+    assert s.min() > 0.999
+    assert np.allclose(Phi.T @ Phi, np.eye(r), atol=1e-10)
+
+
+def test_jacobi_eigh():
+    from cppimpact_gb300 import surrogate as sg
+    rng = np.random.default_rng(2)
+    A = rng.standard_normal((12, 12))
+    A = A + A.T
+    w, V = sg.jacobi_eigh(A)
+    wr = np.sort(np.linalg.eigvalsh(A))[::-1]
+    assert np.allclose(w, wr, atol=1e-10)
+    assert np.allclose(V @ np.diag(w) @ V.T, A, atol=1e-9)
+
+
+def test_snapshots_match_final_state(cilib):
+    torch = pytest.importorskip("torch")
+    from cppimpact_gb300 import surrogate as sg
+    cfg = sg.Config(n_cube=3, steps=200, every=50)
+    params = sg.sample_params(3, np.random.default_rng(9))
+    snaps, peak_ep, ms = sg.generate(params, cfg)
+    assert snaps.shape == (3, 4, 3 * 64)
+    # the last snapshot (after all 200 steps) is the unbatched solver's end state
+    # rounded to FP32 (x - X recomputed in FP64 may differ by one FP32 rounding)
+    from cppimpact_gb300 import meshgen as mg
+    from cppimpact_gb300.sweep import tilted_setup
+    m = mg.cube(3, 1)
+    for i, (v, sy, h, tilt) in enumerate(params):
+        st = tilted_setup(m, v, tilt)
+        s = cilib.Solver(m.xloc, m.conn, E=sg.E, nu=sg.NU, rho=sg.RHO, sigma_y0=sy, H=h * sg.E,
+                         wall_normal=st["wall_normal"], wall_offset=st["wall_offset"],
+                         wall_stiffness=st["wall_stiffness"])
+        s.initialize(st["vel"])
+        s.start(st["dt"])
+        s.step(200)
+        u = (s.state(fields=("x",))["x"] - m.xloc).reshape(-1)
+        got = snaps[i, -1].cpu().numpy().astype(np.float64)
+        assert np.abs(got - u).max() <= 2e-7 * np.abs(u).max() + 1e-15
+
+
+def test_small_surrogate_end_to_end(cilib):
+    pytest.importorskip("torch")
+    from cppimpact_gb300 import surrogate as sg
+    cfg = sg.Config(n_cube=4, steps=400, every=50, rank=8, hidden=64, n_train=96, n_test=16,
+                    epochs=150, batch=32, ensemble=2)
+    rng = np.random.default_rng(cfg.seed)
+    ptr, pte = sg.sample_params(cfg.n_train, rng), sg.sample_params(cfg.n_test, rng)
+    s_tr, _, _ = sg.generate(ptr, cfg)
+    s_te, _, _ = sg.generate(pte, cfg)
+    sur = sg.Surrogate(cfg)
+    sur.fit(ptr, s_tr)
+    assert sur.pod_error < 0.05
+    truth = sg.peak_disp(s_te).cpu().numpy()
+    mean, spread = sur.predict(pte)
+    err = np.abs(mean.cpu().numpy() - truth) / truth
+    assert np.all(np.isfinite(err)) and np.median(err) < 0.2
