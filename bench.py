@@ -1,6 +1,6 @@
 """Benchmark of the explicit impact step: element-steps/s on one GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload shell|quad|small]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload shell|quad|small|surrogate]
                     [--impl ours|reference]
 
 Default workload: the large thin shell -- a cylinder R = 1 m, L = 4 m, t = 4 mm,
@@ -288,8 +288,10 @@ def run_sweep(args, count=256, sample=16):
     inst = sweep.make_instances(count)
     t_gen = time.perf_counter() - t0
     t0 = time.perf_counter()
-    b = api.Batch(inst)
+    b = api.Batch(inst, autotune_steps=args.autotune)
     t_create = time.perf_counter() - t0
+    tuning = {f"tet{npe}": b.tuning(npe) for npe in (4, 10)
+              if any(d["conn"].shape[1] == npe for d in inst)}
     b.run()  # warm-up run
     ms = b.run()
     def nsteps(d):
@@ -299,17 +301,21 @@ def run_sweep(args, count=256, sample=16):
             t += d["dt"]
         return n
     el_steps = sum(d["conn"].shape[0] * nsteps(d) for d in inst)
-    b.close()
-    # the plain solver: same instances one at a time (sampled)
-    single_ms = []
-    for d in inst[:sample]:
+    # the plain solver (default tile shape): same instances one at a time (sampled);
+    # its end states check the tuned batch (which may differ by FP32 rounding only)
+    single_ms, rel = [], []
+    for i, d in enumerate(inst[:sample]):
         s = api.Solver(d["xloc"], d["conn"], E=d["E"], nu=d["nu"], rho=d["rho"],
                        sigma_y0=d["sigma_y0"], H=d["H"], wall_normal=d["wall_normal"],
                        wall_offset=d["wall_offset"], wall_stiffness=d["wall_stiffness"])
         s.initialize(d["vel"])
         s.start(d["dt"])
         single_ms.append(s.time_steps(nsteps(d)))
+        up = s.state(fields=("x",))["x"] - d["xloc"]
+        ub = b.state(i)["x"] - d["xloc"]
+        rel.append(float(np.linalg.norm(ub - up) / max(np.linalg.norm(up), 1e-300)))
         s.close()
+    b.close()
     frac = sum(d["conn"].shape[0] for d in inst[:sample]) / sum(d["conn"].shape[0] for d in inst)
     plain_ms = sum(single_ms) / max(frac, 1e-12)
     return {"instances": count, "t_end_s": 2e-3, "batch_device_ms": ms,
@@ -317,9 +323,49 @@ def run_sweep(args, count=256, sample=16):
             "plain_gpu_runs_per_hour": count / (plain_ms / 1e3) * 3600.0,
             "speedup_vs_plain_gpu": plain_ms / ms,
             "element_steps_per_s": el_steps / (ms / 1e3),
-            "plain_sample": sample, "setup_s": {"meshes": round(t_gen, 2), "plans": round(t_create, 2)},
-            "peak_disp_err_vs_unbatched": 0.0,
-            "note": "each instance is bitwise its unbatched run (tests/test_gpu_batch.py)"}
+            "plain_sample": sample,
+            "setup_s": {"meshes": round(t_gen, 2), "plans_and_autotune": round(t_create, 2)},
+            "autotune_steps": args.autotune, "tuning": tuning,
+            "end_disp_rel_l2_vs_plain_max": max(rel),
+            "note": "with the same tile shape each instance is bitwise its unbatched run "
+                    "(tests/test_gpu_batch.py); the tuned shape differs from the plain "
+                    "solver's default only by FP32 rounding (end_disp_rel_l2_vs_plain_max)"}
+
+
+def run_surrogate(args, rank, world):
+    """The learned-surrogate sweep (4096 training runs of the 12^3 x 6 tet4 cube, POD rank
+    64, MLP 4-256-256-5120, 512 held-out parameter sets with audit and fallback): runs per
+    hour against the plain GPU solver, errors against the solver, and the tensor-core
+    roofline of the largest BF16 GEMM."""
+    from cppimpact_gb300 import surrogate as sg
+    if rank != 0:
+        return None
+    cfg = sg.Config()
+    with ClockSampler(0) as clk:
+        r = sg.study(cfg)
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        peaks = {}
+    peak = peaks.get("bf16_tflops", 1900.0)
+    g = r["gemm"]
+    rph = r["runs_per_hour"]
+    return {
+        "metric": "surrogate sweep runs/hr vs plain GPU solver at <=2% peak-disp err",
+        "value": rph["surrogate"], "unit": "runs/h", "n_gpus": 1, "steps": cfg.steps,
+        "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 GEMM / f32 solver", "data": "synthetic (seeded parameters)",
+        "config": {"workload": f"surrogate: cube {cfg.n_cube}^3x6 tet4, {cfg.n_train} training runs, "
+                               f"{cfg.n_test} held-out, snapshots every {cfg.every} of {cfg.steps} steps, "
+                               f"POD rank {cfg.rank}, MLP 4-{cfg.hidden}-{cfg.hidden}-{cfg.rank * cfg.snaps}"},
+        "speedup_vs_plain_gpu": r["speedup_vs_plain_gpu"],
+        "roofline": {"bound": "tensor", "kernel": "k_gemm_bf16 (POD projection S^T Q)",
+                     "achieved": round(g["tflops"], 2), "peak": peak, "unit": "TFLOP/s",
+                     "frac": round(g["tflops"] / peak, 4),
+                     "peak_source": "measured" if "bf16_tflops" in peaks else "fallback",
+                     "traffic": None},
+        "surrogate": r, "clocks": clk.summary(),
+    }
 
 
 def run_reference(args, rank, world):
@@ -369,7 +415,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--warmup", type=int, default=20)
-    ap.add_argument("--workload", default="shell", choices=["shell", "shell_half", "quad", "small"])
+    ap.add_argument("--workload", default="shell",
+                    choices=["shell", "shell_half", "quad", "small", "surrogate"])
     ap.add_argument("--step-kernel", type=int, default=0, help="0 fused, 1 element + node kernels")
     ap.add_argument("--chunk-elements", type=int, default=0)
     ap.add_argument("--chunk-nodes", type=int, default=0)
@@ -380,12 +427,18 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep", type=int, default=1, help="also run the 256-instance batched sweep")
+    ap.add_argument("--autotune", type=int, default=128,
+                    help="sweep: trial steps per candidate tile shape (0 = default shape)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per element-kernel launch from an ncu capture")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world = dist_setup(args.gpus)
-    if args.impl == "reference":
+    if args.workload == "surrogate":
+        line = ({"impl": "reference", "unavailable": "the reference has no surrogate; the "
+                 "comparison is the plain GPU solver inside our line"}
+                if args.impl == "reference" else run_surrogate(args, rank, world))
+    elif args.impl == "reference":
         line = run_reference(args, rank, world)
     else:
         line = run_ours(args, rank, world)

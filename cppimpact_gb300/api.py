@@ -21,7 +21,9 @@ import os
 import numpy as np
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_PKG, "libcppimpact_gb300.so")
+# CPPIMPACT_GB300_LIB selects another build of the library (e.g. one configured with
+# different compile-time options by ``python -m cppimpact_gb300.build --out``)
+LIB_PATH = os.environ.get("CPPIMPACT_GB300_LIB") or os.path.join(_PKG, "libcppimpact_gb300.so")
 
 CI_OK = 0
 ERRORS = {-1: "CI_ERR_INVALID", -2: "CI_ERR_CUDA", -3: "CI_ERR_DEGENERATE",
@@ -56,7 +58,7 @@ class CiOptions(C.Structure):
     _fields_ = [("mode", C.c_int), ("lumping", C.c_int), ("gravity", C.c_double * 3),
                 ("device", C.c_int), ("chunk_elements", C.c_int), ("chunk_nodes", C.c_int),
                 ("graph_steps", C.c_int), ("step_kernel", C.c_int), ("block_threads", C.c_int),
-                ("elem_lanes", C.c_int)]
+                ("elem_lanes", C.c_int), ("autotune_steps", C.c_int)]
 
 
 class CiInstance(C.Structure):
@@ -105,6 +107,7 @@ EXPORTS = {
     "ci_batch_get_state": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _fp, _ubp,
                                      C.POINTER(C.c_longlong)]),
     "ci_batch_destroy": (C.c_int, [C.c_void_p]),
+    "ci_batch_tuning": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _fp]),
     "ci_batch_run_snapshots": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, _fp]),
     "ci_batch_node_order": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip]),
     "ci_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
@@ -324,11 +327,15 @@ class Batch:
     wall_offset, wall_stiffness, vel, dt, t_end (and optionally pos)."""
 
     def __init__(self, instances, *, gravity=(0.0, 0.0, -9.81), device=0, chunk_nodes=0,
-                 block_threads=0, elem_lanes=0):
+                 block_threads=0, elem_lanes=0, autotune_steps=0):
         self._meshes = []
         arr = (CiInstance * len(instances))()
+        shared = {}  # instances passing the same arrays share one copy (and one plan)
         for i, d in enumerate(instances):
-            m = MeshArrays(d["xloc"], d["conn"])
+            key = (id(d["xloc"]), id(d["conn"]))
+            if key not in shared:
+                shared[key] = MeshArrays(d["xloc"], d["conn"])
+            m = shared[key]
             self._meshes.append(m)
             arr[i].mesh = m.c
             arr[i].mat = CiMaterial(d["E"], d["nu"], d["rho"], d.get("sigma_y0", 0.0),
@@ -344,10 +351,19 @@ class Batch:
         opt.gravity = (C.c_double * 3)(*gravity)
         opt.device, opt.chunk_nodes = device, chunk_nodes
         opt.block_threads, opt.elem_lanes = block_threads, elem_lanes
+        opt.autotune_steps = autotune_steps
         self._arr = arr
         self._h = C.c_void_p()
         check(lib().ci_batch_create(arr, len(instances), C.byref(opt), C.byref(self._h)))
         self.n = len(instances)
+
+    def tuning(self, npe) -> dict:
+        """Tile shape of the group of npe-node elements (the autotuner's choice if tuned)."""
+        cn, bs, ln, ms = C.c_int(0), C.c_int(0), C.c_int(0), C.c_float(0)
+        check(lib().ci_batch_tuning(self._h, npe, C.byref(cn), C.byref(bs), C.byref(ln),
+                                    C.byref(ms)))
+        return dict(chunk_nodes=cn.value, block_threads=bs.value, elem_lanes=ln.value,
+                    trial_ms_per_step=ms.value)
 
     def run(self) -> float:
         """Runs every instance to its end time; returns the batch's device time in ms."""

@@ -36,20 +36,25 @@ def _stale(obj: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, extra_nvcc: list[str] | None = None, out: str | None = None,
+          build_dir: str | None = None) -> str:
+    """Compile and link; ``extra_nvcc`` flags (e.g. -D options) go to every CUDA unit,
+    ``out`` / ``build_dir`` place a differently configured library elsewhere."""
+    lib_path = out or LIB
+    bdir = build_dir or BUILD
+    os.makedirs(bdir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "cppimpact_gb300.h"))
     jobs, objs = [], []
     for src in HOST_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(bdir, src + ".o")
         objs.append(o)
         if _stale(o, [s] + headers):
             jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-c", s, "-o", o])
     for src in CUDA_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(bdir, src + ".o")
         objs.append(o)
         if _stale(o, [s] + headers):
             jobs.append([_nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -64,13 +69,20 @@ def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
         failed |= p.returncode != 0
     if failed:
         raise RuntimeError("libcppimpact_gb300 build failed")
-    if jobs or not os.path.exists(LIB):
-        link = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    if jobs or not os.path.exists(lib_path):
+        link = [_nvcc(), *ARCH, "-shared", "-o", lib_path, *objs, "-lcudart"]
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
-    return LIB
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("-v", action="store_true")
+    ap.add_argument("-D", action="append", default=[], help="preprocessor define for CUDA units")
+    ap.add_argument("--out", default=None, help="library path (default: in-tree)")
+    ap.add_argument("--build-dir", default=None)
+    a = ap.parse_args()
+    print(build(verbose=a.v, extra_nvcc=[f"-D{d}" for d in a.D], out=a.out, build_dir=a.build_dir))

@@ -17,6 +17,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/cppimpact_gb300.h"
@@ -82,7 +83,8 @@ struct Group {
   long long S = 0, Lt = 0;
   int max_local = 0;
   size_t smem = 0;
-  int block_threads = 128, elem_lanes = 4, chunk_nodes = 1024;
+  int block_threads = 128, elem_lanes = 4, chunk_nodes = 896;
+  float tuned_ms_per_step = 0.f;  // autotuner's trial time of the chosen shape (0: not tuned)
   std::vector<int> insts;  // global instance ids
   int max_steps = 0;
   cudaStream_t stream = nullptr;
@@ -241,30 +243,65 @@ cudaError_t configure(int bytes) {
 
 // Build one element-type group from its instances.
 int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& opt) {
-  std::vector<Plan> plans(G.insts.size());
-  std::string err;
-  for (size_t j = 0; j < G.insts.size(); j++) {
-    const ci_instance& I = in[G.insts[j]];
-    if (!build_plan(I.mesh.num_nodes, I.mesh.num_elements, I.mesh.nodes_per_element, I.mesh.xloc,
-                    I.mesh.element_nodes, opt.chunk_elements, G.chunk_nodes, 304, &plans[j], &err))
-      return fail(CI_ERR_INVALID, "instance " + std::to_string(G.insts[j]) + ": " + err);
+  // Instances that pass the same mesh arrays share one plan (a parameter sweep over
+  // one mesh plans it once); distinct meshes are planned on the host's cores.
+  const size_t n_inst = G.insts.size();
+  std::vector<size_t> src(n_inst), uniq;
+  for (size_t j = 0; j < n_inst; j++) {
+    const ci_mesh& a = in[G.insts[j]].mesh;
+    src[j] = j;
+    for (size_t u : uniq) {
+      const ci_mesh& m = in[G.insts[u]].mesh;
+      if (m.xloc == a.xloc && m.element_nodes == a.element_nodes && m.num_nodes == a.num_nodes &&
+          m.num_elements == a.num_elements && m.nodes_per_element == a.nodes_per_element) {
+        src[j] = u;
+        break;
+      }
+    }
+    if (src[j] == j) uniq.push_back(j);
   }
+  std::vector<Plan> built(n_inst);
+  std::vector<std::string> errs(n_inst);
+  std::vector<char> ok(n_inst, 0);
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t n_thr = std::min<size_t>(std::min<size_t>(hw, 32), uniq.size());
+  auto work = [&](size_t t) {
+    for (size_t i = t; i < uniq.size(); i += n_thr) {
+      const size_t j = uniq[i];
+      const ci_instance& I = in[G.insts[j]];
+      ok[j] = build_plan(I.mesh.num_nodes, I.mesh.num_elements, I.mesh.nodes_per_element,
+                         I.mesh.xloc, I.mesh.element_nodes, opt.chunk_elements, G.chunk_nodes, 304,
+                         &built[j], &errs[j]);
+    }
+  };
+  if (n_thr <= 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < n_thr; t++) th.emplace_back(work, t);
+    for (auto& t : th) t.join();
+  }
+  for (size_t u : uniq)
+    if (!ok[u]) return fail(CI_ERR_INVALID, "instance " + std::to_string(G.insts[u]) + ": " + errs[u]);
+  std::vector<const Plan*> plans(n_inst);
+  for (size_t j = 0; j < n_inst; j++) plans[j] = &built[src[j]];
   // sizes and offsets
   G.N = G.E = G.C = 0;
   G.S = G.Lt = 0;
   G.max_local = 0;
   for (size_t j = 0; j < plans.size(); j++) {
     Inst& T = b->inst[G.insts[j]];
+    const Plan& P = *plans[j];
     T.node_off = G.N;
     T.elem_off = G.E;
-    T.node_orig = plans[j].node_orig;
-    T.elem_orig = plans[j].elem_orig;
-    G.N += plans[j].N;
-    G.E += plans[j].E;
-    G.C += plans[j].n_chunks;
-    G.S += plans[j].slot_row[plans[j].N];
-    G.Lt += (long long)plans[j].local_gid.size();
-    G.max_local = std::max(G.max_local, plans[j].max_local);
+    T.node_orig = P.node_orig;
+    T.elem_orig = P.elem_orig;
+    G.N += P.N;
+    G.E += P.E;
+    G.C += P.n_chunks;
+    G.S += P.slot_row[P.N];
+    G.Lt += (long long)P.local_gid.size();
+    G.max_local = std::max(G.max_local, P.max_local);
   }
   const int npe = G.npe;
   std::vector<ChunkInfo> chunks;
@@ -280,7 +317,7 @@ int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& 
   slot_row.reserve(G.N + 1);
   G.max_steps = 0;
   for (size_t j = 0; j < plans.size(); j++) {
-    const Plan& P = plans[j];
+    const Plan& P = *plans[j];
     Inst& T = b->inst[G.insts[j]];
     for (ChunkInfo c : P.chunks) {
       c.elem_begin += T.elem_off;
@@ -473,6 +510,70 @@ int enqueue_run_graph(Group& G, int total, int per_graph) {
   return CI_OK;
 }
 
+// Project autotuner: time `steps` steps of every candidate tile shape -- local-node
+// budget per chunk (plan), CTA size, lanes per tet10 element -- on the group's own
+// instances from their initial state, and keep the fastest.  Options fixed by the
+// caller are not varied.  The group is left built with the winner (graph not captured).
+int autotune_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& opt) {
+  std::vector<int> cns = opt.chunk_nodes ? std::vector<int>{opt.chunk_nodes}
+                                         : std::vector<int>{512, 768, 896, 1024};
+  std::vector<int> bss = opt.block_threads ? std::vector<int>{opt.block_threads}
+                                           : std::vector<int>{64, 128, 256};
+  std::vector<int> lanes = (G.npe == 4 || opt.elem_lanes) ? std::vector<int>{G.elem_lanes}
+                                                          : std::vector<int>{1, 4};
+  const int graphs = std::max(1, (opt.autotune_steps + kGraphSteps - 1) / kGraphSteps);
+  cudaEvent_t e0, e1;
+  CB_CUDA(cudaEventCreate(&e0));
+  CB_CUDA(cudaEventCreate(&e1));
+  struct Ev {
+    cudaEvent_t a, b;
+    ~Ev() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } ev{e0, e1};
+  float best = 0.f;
+  int best_cn = cns[0], best_bs = bss[0], best_ln = lanes[0];
+  for (int cn : cns) {
+    G.chunk_nodes = cn;
+    int rc = build_group(b, G, in, opt);
+    if (rc) return rc;
+    for (int bs : bss)
+      for (int ln : lanes) {
+        G.block_threads = bs;
+        G.elem_lanes = ln;
+        if ((rc = capture_graph(G))) return rc;
+        if ((rc = enqueue_run(G, false))) return rc;
+        CB_CUDA(cudaGraphLaunch(G.graph, G.stream));  // warm-up: uploads the graph
+        CB_CUDA(cudaEventRecord(e0, G.stream));
+        for (int r = 0; r < graphs; r++) CB_CUDA(cudaGraphLaunch(G.graph, G.stream));
+        CB_CUDA(cudaEventRecord(e1, G.stream));
+        CB_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        unsigned int st = 0;
+        CB_CUDA(cudaMemcpy(&st, G.status.p, sizeof(st), cudaMemcpyDeviceToHost));
+        if (st & ST_DEGENERATE) return fail(CI_ERR_DEGENERATE, "an element has det J <= 0");
+        if (st & ST_NONFINITE) return fail(CI_ERR_NONFINITE, "non-finite nodal state");
+        ms /= (float)(graphs * kGraphSteps);
+        if (best == 0.f || ms < best) {
+          best = ms;
+          best_cn = cn;
+          best_bs = bs;
+          best_ln = ln;
+        }
+      }
+  }
+  G.block_threads = best_bs;
+  G.elem_lanes = best_ln;
+  G.tuned_ms_per_step = best;
+  if (G.chunk_nodes != best_cn) {
+    G.chunk_nodes = best_cn;
+    return build_group(b, G, in, opt);
+  }
+  return CI_OK;
+}
+
 // Displacement of every node after k = *step_ctr global steps, FP32, into
 // snap[(k / every - 1)][node][3] (plan order).  Interior nodes of an instance still
 // stepping hold S^k in buffer k & 1; its boundary nodes are completed from S^{k-1} and
@@ -570,9 +671,14 @@ int ci_batch_create(const ci_instance* inst, int n, const ci_options* opt_in, ci
     if (G->insts.empty()) continue;
     G->block_threads = opt.block_threads ? opt.block_threads : 128;
     G->elem_lanes = opt.elem_lanes ? opt.elem_lanes : 4;
-    G->chunk_nodes = opt.chunk_nodes ? opt.chunk_nodes : 1024;
+    G->chunk_nodes = opt.chunk_nodes ? opt.chunk_nodes : 896;
+    if (G->block_threads != 64 && G->block_threads != 128 && G->block_threads != 256)
+      return fail(CI_ERR_INVALID, "block_threads must be 64, 128 or 256");
+    if (G->elem_lanes != 1 && G->elem_lanes != 4)
+      return fail(CI_ERR_INVALID, "elem_lanes must be 1 or 4");
     CB_CUDA(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
-    int rc = build_group(b.get(), *G, inst, opt);
+    int rc = opt.autotune_steps > 0 ? autotune_group(b.get(), *G, inst, opt)
+                                    : build_group(b.get(), *G, inst, opt);
     if (rc) return rc;
     if ((rc = capture_graph(*G))) return rc;
     b->g[gi] = std::move(G);
@@ -617,6 +723,18 @@ int ci_batch_run(ci_batch* b, float* device_ms) {
       if (st & ST_NONFINITE) return fail(CI_ERR_NONFINITE, "non-finite nodal state");
     }
   b->done = true;
+  return CI_OK;
+}
+
+int ci_batch_tuning(ci_batch* b, int npe, int* chunk_nodes, int* block_threads, int* elem_lanes,
+                    float* trial_ms_per_step) {
+  if (!b || (npe != 4 && npe != 10)) return fail(CI_ERR_INVALID, "ci_batch_tuning: bad arguments");
+  const Group* G = b->g[npe == 4 ? 0 : 1].get();
+  if (!G) return fail(CI_ERR_INVALID, "ci_batch_tuning: the batch has no instance of that type");
+  if (chunk_nodes) *chunk_nodes = G->chunk_nodes;
+  if (block_threads) *block_threads = G->block_threads;
+  if (elem_lanes) *elem_lanes = G->npe == 10 ? G->elem_lanes : 1;
+  if (trial_ms_per_step) *trial_ms_per_step = G->tuned_ms_per_step;
   return CI_OK;
 }
 

@@ -852,21 +852,36 @@ __device__ __forceinline__ void tet10_gather(const Tet10QP& t, const Tile& T, in
   }
 }
 
+// Force component c of node I at this lane's point (I < 0: none).
 template <int I>
-__device__ __forceinline__ void tet10_node_force(const Tet10QP& t, const float (&Pm)[9], int q,
-                                                 float (&keep)[3][3]) {
-  float f[3];
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    float v = tet10_force<I>(t, &Pm[3 * a]);
-    v += __shfl_xor_sync(0xffffffffu, v, 1);
-    v += __shfl_xor_sync(0xffffffffu, v, 2);
-    f[a] = v;
+__device__ __forceinline__ float tet10_fc(const Tet10QP& t, const float (&Pm)[9], int c) {
+  if (I < 0) return 0.f;
+  return tet10_force<(I < 0 ? 0 : I)>(t, &Pm[3 * c]);
+}
+
+// Sum over the 4 lanes of an element (its 4 points) of the forces of the nodes lane q
+// owns, delivered to lane q only: R[0..2] node q, R[3..5] node q + 4, R[6..8] node
+// q + 8 (q < 2).  Two butterfly levels: xor 2 leaves lanes 0, 1 with nodes
+// {0,4,8,1,5,9} and lanes 2, 3 with {2,6,3,7}; xor 1 splits each pair.
+template <int K>
+__device__ __forceinline__ void tet10_rs_slot(const Tet10QP& t, const float (&Pm)[9], bool lo,
+                                              bool even, float (&R)[9]) {
+  constexpr int r = K / 3, c = K % 3;
+  constexpr int L0 = r == 0 ? 0 : r == 1 ? 4 : 8;
+  constexpr int L1 = r == 0 ? 1 : r == 1 ? 5 : 9;
+  constexpr int H0 = r == 0 ? 2 : r == 1 ? 6 : -1;
+  constexpr int H1 = r == 0 ? 3 : r == 1 ? 7 : -1;
+  const float a0 = tet10_fc<L0>(t, Pm, c), a1 = tet10_fc<L1>(t, Pm, c);
+  float m0, m1;
+  if (H0 >= 0) {
+    const float b0 = tet10_fc<H0>(t, Pm, c), b1 = tet10_fc<H1>(t, Pm, c);
+    m0 = (lo ? a0 : b0) + __shfl_xor_sync(0xffffffffu, lo ? b0 : a0, 2);
+    m1 = (lo ? a1 : b1) + __shfl_xor_sync(0xffffffffu, lo ? b1 : a1, 2);
+  } else {
+    m0 = a0 + __shfl_xor_sync(0xffffffffu, a0, 2);
+    m1 = a1 + __shfl_xor_sync(0xffffffffu, a1, 2);
   }
-  if ((I & 3) == q) {
-#pragma unroll
-    for (int a = 0; a < 3; a++) keep[I >> 2][a] = f[a];
-  }
+  R[K] = (even ? m0 : m1) + __shfl_xor_sync(0xffffffffu, even ? m1 : m0, 1);
 }
 
 template <int MODE, int BS, bool BATCH = false>
@@ -967,16 +982,21 @@ __global__ void __launch_bounds__(BS) k_step_qp10(FusedArgs A, ElemParams ep_arg
         Pm[3 * a + j] = wd * (Sg[3 * a + 0] * Ji[3 * j + 0] + Sg[3 * a + 1] * Ji[3 * j + 1] +
                               Sg[3 * a + 2] * Ji[3 * j + 2]);
     float keep[3][3];
-    tet10_node_force<0>(t, Pm, q, keep);
-    tet10_node_force<1>(t, Pm, q, keep);
-    tet10_node_force<2>(t, Pm, q, keep);
-    tet10_node_force<3>(t, Pm, q, keep);
-    tet10_node_force<4>(t, Pm, q, keep);
-    tet10_node_force<5>(t, Pm, q, keep);
-    tet10_node_force<6>(t, Pm, q, keep);
-    tet10_node_force<7>(t, Pm, q, keep);
-    tet10_node_force<8>(t, Pm, q, keep);
-    tet10_node_force<9>(t, Pm, q, keep);
+    {
+      float R[9];
+      const bool lo = q < 2, even = (q & 1) == 0;
+      tet10_rs_slot<0>(t, Pm, lo, even, R);
+      tet10_rs_slot<1>(t, Pm, lo, even, R);
+      tet10_rs_slot<2>(t, Pm, lo, even, R);
+      tet10_rs_slot<3>(t, Pm, lo, even, R);
+      tet10_rs_slot<4>(t, Pm, lo, even, R);
+      tet10_rs_slot<5>(t, Pm, lo, even, R);
+      tet10_rs_slot<6>(t, Pm, lo, even, R);
+      tet10_rs_slot<7>(t, Pm, lo, even, R);
+      tet10_rs_slot<8>(t, Pm, lo, even, R);
+#pragma unroll
+      for (int k = 0; k < 9; k++) keep[k / 3][k % 3] = R[k];
+    }
     // lane q owns nodes q, q+4 and (for q < 2) q+8
     const int own0 = q == 0 ? ln[0] : q == 1 ? ln[1] : q == 2 ? ln[2] : ln[3];
     const int own1 = q == 0 ? ln[4] : q == 1 ? ln[5] : q == 2 ? ln[6] : ln[7];

@@ -83,7 +83,7 @@ bool build_plan(int N, int E, int npe, const double* xloc, const int* conn, int 
   if (target_ctas <= 0) target_ctas = 304;
   int emax = chunk_elements > 0 ? chunk_elements
                                 : std::max(32, std::min(4096, (E + target_ctas - 1) / target_ctas));
-  int lmax = chunk_nodes > 0 ? chunk_nodes : 1024;
+  int lmax = chunk_nodes > 0 ? chunk_nodes : 896;
   lmax = std::max(lmax, npe);
   std::vector<int> stamp(N, -1), owner(N, -1), touch(N, 0);
   std::vector<int> cbeg;  // chunk start in sfc order

@@ -241,8 +241,9 @@ class Surrogate:
         self.mesh = mg.cube(cfg.n_cube, 1)
         self.timings = {}
 
-    def fit(self, params: np.ndarray, snaps):
-        """params [n x 4], snaps [n, snaps, 3N] (torch FP32)."""
+    def fit(self, params: np.ndarray, snaps, peak_ep=None):
+        """params [n x 4], snaps [n, snaps, 3N] (torch FP32), peak_ep [n] (peak equivalent
+        plastic strain; optional: the networks then predict it as one more output)."""
         torch = _torch()
         cfg = self.cfg
         n, k, d = snaps.shape
@@ -258,19 +259,43 @@ class Surrogate:
                     / S.float().norm())
         self.pod_error = rel
         Y = A.view(n, k * cfg.rank)
+        # one scale for all modal outputs: the squared error of the normalised output is
+        # then proportional to the squared error of the reconstructed displacement field
         self.y_mean = Y.mean(dim=0, keepdim=True)
-        self.y_std = Y.std(dim=0, keepdim=True) + 1e-12 * Y.abs().max()
+        self.y_std = (Y - self.y_mean).std() + 1e-30
         Yn = ((Y - self.y_mean) / self.y_std).contiguous()
         X = torch.tensor(normalise(params), device="cuda")
         self.train_X, self.train_Y = X, Y
         t0 = time.perf_counter()
         self.nets, self.losses = [], []
         for j in range(cfg.ensemble):
-            net = MLP(4, cfg.hidden, k * cfg.rank, cfg.seed + 101 * j)
-            self.losses.append(net.train(X, Yn, cfg.epochs, cfg.batch, cfg.lr, cfg.seed + 7 * j))
+            net = MLP(4, cfg.hidden, Yn.shape[1], cfg.seed + 101 * j)
+            self.losses.append(self._train(net, X, Yn, cfg.seed + 7 * j))
             self.nets.append(net)
+        # peak equivalent plastic strain: a smaller network per ensemble member
+        self.with_ep = peak_ep is not None
+        self.ep_nets = []
+        if self.with_ep:
+            ep = torch.tensor(np.asarray(peak_ep, dtype=np.float32), device="cuda")[:, None]
+            self.ep_mean, self.ep_std = ep.mean(), ep.std() + 1e-30
+            self.train_ep = ep[:, 0]
+            Tn = ((ep - self.ep_mean) / self.ep_std).contiguous()
+            for j in range(cfg.ensemble):
+                net = MLP(4, 64, 1, cfg.seed + 303 * j)
+                self._train(net, X, Tn, cfg.seed + 11 * j)
+                self.ep_nets.append(net)
         torch.cuda.synchronize()
         self.timings["train_s"] = time.perf_counter() - t0
+
+    def _train(self, net, X, T, seed):
+        """Adam in three phases of decreasing step size (lr, lr/5, lr/25)."""
+        cfg = self.cfg
+        parts = [cfg.epochs // 2, cfg.epochs // 4, cfg.epochs - cfg.epochs // 2 - cfg.epochs // 4]
+        losses = []
+        for i, (ep, lr) in enumerate(zip(parts, (cfg.lr, cfg.lr / 5, cfg.lr / 25))):
+            if ep > 0:
+                losses.append(net.train(X, T, ep, cfg.batch, lr, seed + 1000 * i))
+        return np.concatenate(losses)
 
     def _reconstruct_peak(self, A):
         """A [n, snaps * r] modal trajectories -> peak displacement per run."""
@@ -280,8 +305,9 @@ class Surrogate:
         U = gemm(A.view(n * k, r).to(torch.bfloat16).contiguous(), self.Phib, transB=True)
         return peak_disp(U.view(n, k, -1))
 
-    def predict(self, params: np.ndarray):
-        """Ensemble prediction: (peak displacement mean, relative spread) per query."""
+    def predict(self, params: np.ndarray, with_ep: bool = False):
+        """Ensemble prediction: (peak displacement mean, relative spread) per query, and
+        the ensemble-mean peak equivalent plastic strain when ``with_ep``."""
         torch = _torch()
         X = torch.tensor(normalise(params), device="cuda")
         peaks = []
@@ -291,7 +317,13 @@ class Surrogate:
         P = torch.stack(peaks)
         mean = P.mean(dim=0)
         spread = P.std(dim=0) / mean.clamp_min(1e-30) if len(peaks) > 1 else torch.zeros_like(mean)
-        return mean, spread
+        if not with_ep:
+            return mean, spread
+        ep = None
+        if self.ep_nets:
+            ep = torch.stack([net.predict(X)[:, 0] for net in self.ep_nets]).mean(dim=0)
+            ep = ep * self.ep_std + self.ep_mean
+        return mean, spread, ep
 
     def predict_idw(self, params: np.ndarray, k_nn: int = 8):
         """The method without the network: inverse-distance-weighted interpolation of the
@@ -303,12 +335,148 @@ class Surrogate:
         w = 1.0 / dist.clamp_min(1e-6) ** 2
         w = w / w.sum(dim=1, keepdim=True)
         A = (self.train_Y[idx] * w[..., None]).sum(dim=1)
+        if getattr(self, "with_ep", False):
+            return self._reconstruct_peak(A), (self.train_ep[idx] * w).sum(dim=1)
         return self._reconstruct_peak(A)
 
 
 def fallback_runs(params: np.ndarray, cfg: Config, mesh=None):
-    """Plain solver for the given queries (one batch); peak displacement, device ms."""
+    """The solver for the given queries (one batch): peak displacement, peak equivalent
+    plastic strain, device ms."""
     if len(params) == 0:
-        return np.zeros(0), 0.0
-    s, _, ms = generate(params, cfg, mesh)
-    return peak_disp(s).cpu().numpy(), ms
+        return np.zeros(0), np.zeros(0), 0.0
+    s, ep, ms = generate(params, cfg, mesh)
+    return peak_disp(s).cpu().numpy(), ep, ms
+
+
+def plain_run_ms(params: np.ndarray, cfg: Config, mesh=None) -> list[float]:
+    """Device time of whole runs of the plain (unbatched) GPU solver, one at a time."""
+    mesh = mesh or mg.cube(cfg.n_cube, 1)
+    out = []
+    for v, sy, h, tilt in params:
+        st = tilted_setup(mesh, v, tilt)
+        s = api.Solver(mesh.xloc, mesh.conn, E=E, nu=NU, rho=RHO, sigma_y0=sy, H=h * E,
+                       wall_normal=st["wall_normal"], wall_offset=st["wall_offset"],
+                       wall_stiffness=st["wall_stiffness"])
+        s.initialize(st["vel"])
+        s.start(st["dt"])
+        out.append(s.time_steps(cfg.steps))
+        s.close()
+    return out
+
+
+def _errstats(e: np.ndarray) -> dict:
+    e = np.asarray(e, dtype=np.float64)
+    if e.size == 0:
+        return {}
+    return dict(mean=float(e.mean()), p50=float(np.median(e)), p95=float(np.quantile(e, 0.95)),
+                max=float(e.max()), frac_over_2pct=float((e > 0.02).mean()))
+
+
+def gemm_tflops(rows: int, dofs: int, k: int, reps: int = 5) -> dict:
+    """Throughput of the POD's largest product, W = S^T Q ([dofs x rows] x [rows x k])."""
+    torch = _torch()
+    S = torch.randn((rows, dofs), device="cuda").to(torch.bfloat16)
+    Q = torch.randn((rows, k), device="cuda").to(torch.bfloat16)
+    out = torch.empty((dofs, k), dtype=torch.float32, device="cuda")
+    gemm(S, Q, transA=True, out=out)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        gemm(S, Q, transA=True, out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    return dict(shape=[dofs, k, rows], ms=ms, tflops=2.0 * rows * dofs * k / (ms * 1e-3) / 1e12)
+
+
+def study(cfg: Config, plain_sample: int = 4, audit_fail_fraction: float = 0.1) -> dict:
+    """The surrogate sweep end to end: training runs, fit, prediction of held-out
+    parameter sets with audit and fallback, errors against the solver, and runs/hour
+    against the plain GPU solver and the batched solver alone."""
+    torch = _torch()
+    rng = np.random.default_rng(cfg.seed)
+    ptr, pte = sample_params(cfg.n_train, rng), sample_params(cfg.n_test, rng)
+    mesh = mg.cube(cfg.n_cube, 1)
+    out = {"config": dataclasses.asdict(cfg), "mesh": {"elements": mesh.num_elements,
+                                                       "nodes": mesh.num_nodes}}
+    t0 = time.perf_counter()
+    s_tr, ep_tr, ms_tr = generate(ptr, cfg, mesh)
+    out["train_runs"] = {"wall_s": time.perf_counter() - t0, "device_ms": ms_tr}
+    t0 = time.perf_counter()
+    s_te, ep_te, ms_te = generate(pte, cfg, mesh)
+    wall_te = time.perf_counter() - t0
+    truth_d, truth_ep = peak_disp(s_te).cpu().numpy(), np.asarray(ep_te)
+    del s_te
+    sur = Surrogate(cfg)
+    t0 = time.perf_counter()
+    sur.fit(ptr, s_tr, ep_tr)
+    out["fit"] = {"wall_s": time.perf_counter() - t0, **sur.timings, "pod_rel_error": sur.pod_error,
+                  "final_loss": [float(l[-1]) for l in sur.losses]}
+    del s_tr
+    torch.cuda.synchronize()
+    # surrogate answers: ensemble prediction, then the solver for flagged + audited queries
+    sur.predict(pte[:8], with_ep=True)   # first use loads the reduction kernels
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mean, spread, ep_pred = sur.predict(pte, with_ep=True)
+    mean, spread, ep_pred = mean.cpu().numpy(), spread.cpu().numpy(), ep_pred.cpu().numpy()
+    t_pred = time.perf_counter() - t0
+    n = len(pte)
+    flagged = spread > cfg.spread_threshold
+    arng = np.random.default_rng(cfg.seed + 1)
+    cand = np.flatnonzero(~flagged)
+    n_audit = min(len(cand), int(math.ceil(cfg.audit_fraction * n)))
+    audit = np.zeros(n, bool)
+    audit[arng.choice(cand, n_audit, replace=False)] = True
+    rerun = flagged | audit
+    t0 = time.perf_counter()
+    fb_d, fb_ep, fb_ms = fallback_runs(pte[rerun], cfg, mesh)
+    t_fb = time.perf_counter() - t0
+    final_d, final_ep = mean.copy(), ep_pred.copy()
+    final_d[rerun], final_ep[rerun] = fb_d, fb_ep
+    in_audit = audit[rerun]            # audited among the re-run queries, in fb_d order
+    aud_err = np.abs(mean[rerun][in_audit] - fb_d[in_audit]) / fb_d[in_audit]
+    full_fallback = bool(n_audit and (aud_err > cfg.error_threshold).mean() > audit_fail_fraction)
+    t_full = 0.0
+    if full_fallback:
+        rest = ~rerun
+        t0 = time.perf_counter()
+        d2, e2, _ = fallback_runs(pte[rest], cfg, mesh)
+        t_full = time.perf_counter() - t0
+        final_d[rest], final_ep[rest] = d2, e2
+    t_sur = t_pred + t_fb + t_full
+    ep_scale = max(float(truth_ep.max()), 1e-30)
+    # the method without the network: inverse-distance interpolation of training runs
+    idw_d, idw_ep = sur.predict_idw(pte)
+    idw_d, idw_ep = idw_d.cpu().numpy(), idw_ep.cpu().numpy()
+    out["errors"] = {
+        "surrogate_only_peak_disp": _errstats(np.abs(mean - truth_d) / truth_d),
+        "final_peak_disp": _errstats(np.abs(final_d - truth_d) / truth_d),
+        "idw_peak_disp": _errstats(np.abs(idw_d - truth_d) / truth_d),
+        "surrogate_only_peak_epbar_abs_over_max": _errstats(np.abs(ep_pred - truth_ep) / ep_scale),
+        "final_peak_epbar_abs_over_max": _errstats(np.abs(final_ep - truth_ep) / ep_scale),
+        "idw_peak_epbar_abs_over_max": _errstats(np.abs(idw_ep - truth_ep) / ep_scale),
+        "peak_epbar_max": ep_scale,
+        "audit_error": _errstats(aud_err),
+    }
+    out["audit"] = {"flagged_by_spread": int(flagged.sum()), "audited": int(n_audit),
+                    "rerun": int(rerun.sum()), "full_fallback": full_fallback}
+    plain = plain_run_ms(pte[:plain_sample], cfg, mesh)
+    plain_ms = float(np.mean(plain))
+    out["timing"] = {"predict_s": t_pred, "fallback_wall_s": t_fb, "fallback_device_ms": fb_ms,
+                     "full_fallback_s": t_full, "surrogate_sweep_s": t_sur,
+                     "batched_sweep_wall_s": wall_te, "batched_sweep_device_ms": ms_te,
+                     "plain_run_device_ms": plain_ms}
+    rph = lambda count, sec: count / max(sec, 1e-12) * 3600.0
+    one_off = out["train_runs"]["wall_s"] + out["fit"]["wall_s"]
+    out["runs_per_hour"] = {
+        "surrogate": rph(n, t_sur),
+        "batched_solver": rph(n, wall_te),
+        "plain_gpu_solver": rph(1, plain_ms / 1e3),
+        "surrogate_incl_training_for_this_sweep": rph(n, t_sur + one_off),
+        "break_even_queries": one_off / max(plain_ms / 1e3 - t_sur / n, 1e-12),
+    }
+    out["speedup_vs_plain_gpu"] = out["runs_per_hour"]["surrogate"] / out["runs_per_hour"]["plain_gpu_solver"]
+    out["gemm"] = gemm_tflops(cfg.n_train * cfg.snaps, 3 * mesh.num_nodes, cfg.rank + 32)
+    return out

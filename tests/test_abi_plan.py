@@ -66,7 +66,7 @@ def test_plan_shell_workload_shape(cilib):
     s = mg.shell()
     assert (s.num_elements, s.num_nodes) == (604800, 1213920)
     st = cilib.plan_stats(s.xloc, s.conn)
-    assert st["max_local"] <= 1024            # default local-node budget per chunk
+    assert st["max_local"] <= 896             # default local-node budget per chunk
     assert st["ghosts"] < 0.30 * s.num_nodes
 
 

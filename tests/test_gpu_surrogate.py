@@ -111,3 +111,20 @@ def test_small_surrogate_end_to_end(cilib):
     mean, spread = sur.predict(pte)
     err = np.abs(mean.cpu().numpy() - truth) / truth
     assert np.all(np.isfinite(err)) and np.median(err) < 0.2
+
+
+def test_small_study_audit_and_fallback(cilib):
+    """The sweep driver on a small case: every flagged or audited query carries the
+    solver's answer, the rest the ensemble's; timings and runs/hour are reported."""
+    pytest.importorskip("torch")
+    from cppimpact_gb300 import surrogate as sg
+    cfg = sg.Config(n_cube=4, steps=400, every=50, rank=8, hidden=64, n_train=96, n_test=40,
+                    epochs=120, batch=32, ensemble=2, audit_fraction=0.1)
+    r = sg.study(cfg, plain_sample=2)
+    a = r["audit"]
+    assert a["audited"] == 4 or a["audited"] == 40 - a["flagged_by_spread"]
+    assert a["rerun"] == a["flagged_by_spread"] + a["audited"]
+    assert r["errors"]["final_peak_disp"]["max"] <= r["errors"]["surrogate_only_peak_disp"]["max"] + 1e-12
+    rph = r["runs_per_hour"]
+    assert rph["surrogate"] > 0 and rph["plain_gpu_solver"] > 0 and rph["batched_solver"] > 0
+    assert r["gemm"]["tflops"] > 0
