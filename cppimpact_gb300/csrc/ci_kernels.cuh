@@ -17,6 +17,7 @@
 #pragma once
 #include <cstdint>
 
+#include "ci_fpconv.h"
 #include "ci_plan.h"
 
 namespace ci {
@@ -546,14 +547,14 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     un[k] = __fma_rn(p.dt, v[k], u[k]);
-    uf[k] = (float)un[k];
+    uf[k] = f64_to_f32(un[k]);
   }
   // |d32 - d| <= 2^-22 (|d0| + |u|_1) for |n_k| <= 1; 1e-6 (1 + ...) covers it
   const float d32 = __fadd_rn(d0f, __fadd_rn(__fmul_rn(p.nf[0], uf[0]),
                                   __fadd_rn(__fmul_rn(p.nf[1], uf[1]), __fmul_rn(p.nf[2], uf[2]))));
   const float margin = 1e-6f * (1.f + fabsf(d0f) + fabsf(uf[0]) + fabsf(uf[1]) + fabsf(uf[2]));
   in_contact = false;
-  double ad[3] = {(double)a[0], (double)a[1], (double)a[2]};
+  double ad[3] = {f32_to_f64(a[0]), f32_to_f64(a[1]), f32_to_f64(a[2])};
   if (!(d32 > margin)) {
     const double d = __fma_rn(p.wall_n[2], un[2], __fma_rn(p.wall_n[1], un[1],
                               __fma_rn(p.wall_n[0], un[0], d0[g])));
@@ -563,7 +564,7 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         ad[k] = __fma_rn(c, p.wall_n[k], ad[k]);
-        a[k] = (float)ad[k];
+        a[k] = f64_to_f32(ad[k]);
       }
     }
   }
@@ -572,7 +573,7 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
     v[k] = __fma_rn(p.dt, ad[k], v[k]);
     u[k] = un[k];
     uf_out[k] = uf[k];
-    vf_out[k] = (float)v[k];
+    vf_out[k] = f64_to_f32(v[k]);
   }
 }
 
@@ -884,8 +885,9 @@ __device__ __forceinline__ void tet10_rs_slot(const Tet10QP& t, const float (&Pm
   R[K] = (even ? m0 : m1) + __shfl_xor_sync(0xffffffffu, even ? m1 : m0, 1);
 }
 
+// 6 CTAs of 128 threads per SM (80 registers) fit the 896-node chunk's shared tile
 template <int MODE, int BS, bool BATCH = false>
-__global__ void __launch_bounds__(BS) k_step_qp10(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
+__global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
   extern __shared__ float sm[];
   const DevPlan& P = A.P;
   const ChunkInfo ch = P.chunks[blockIdx.x];
@@ -1073,7 +1075,7 @@ __global__ void __launch_bounds__(256) k_node_init(NodeArrays A, NodeParams p_ar
   for (int k = 0; k < 3; k++) {
     u[k] = A.u[k][n];
     v[k] = A.v[k][n];
-    uf[k] = (float)u[k];
+    uf[k] = f64_to_f32(u[k]);
     ad[k] = (double)p.gf[k];
   }
   const float d32 = __fadd_rn(d0f[n], __fadd_rn(__fmul_rn(p.nf[0], uf[0]),
@@ -1106,8 +1108,8 @@ __global__ void __launch_bounds__(256) k_node_init(NodeArrays A, NodeParams p_ar
 static __global__ void k_shadows(const double* u, const double* v, float* uf, float* vf, long long n3) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n3) return;
-  uf[i] = (float)u[i];
-  vf[i] = (float)v[i];
+  uf[i] = f64_to_f32(u[i]);
+  vf[i] = f64_to_f32(v[i]);
 }
 
 // Adds n to the batched step counter (after each captured block of steps).

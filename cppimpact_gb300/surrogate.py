@@ -44,7 +44,7 @@ class Config:
     hidden: int = 256
     n_train: int = 4096
     n_test: int = 512
-    epochs: int = 300
+    epochs: int = 600
     batch: int = 256
     lr: float = 2e-3
     ensemble: int = 3
@@ -258,9 +258,10 @@ class Surrogate:
         rel = float((S.float() - gemm(A.to(torch.bfloat16).contiguous(), self.Phib, transB=True)).norm()
                     / S.float().norm())
         self.pod_error = rel
-        Y = A.view(n, k * cfg.rank)
-        # one scale for all modal outputs: the squared error of the normalised output is
-        # then proportional to the squared error of the reconstructed displacement field
+        # modal trajectories per unit impact speed (displacements scale with it), then
+        # one scale for all outputs: the squared error of a normalised output is then
+        # proportional to the error of the reconstructed displacement relative to v t
+        Y = A.view(n, k * cfg.rank) / self._speed(params)[:, None]
         self.y_mean = Y.mean(dim=0, keepdim=True)
         self.y_std = (Y - self.y_mean).std() + 1e-30
         Yn = ((Y - self.y_mean) / self.y_std).contiguous()
@@ -287,6 +288,11 @@ class Surrogate:
         torch.cuda.synchronize()
         self.timings["train_s"] = time.perf_counter() - t0
 
+    @staticmethod
+    def _speed(params):
+        torch = _torch()
+        return torch.tensor(np.asarray(params, dtype=np.float32)[:, 0], device="cuda")
+
     def _train(self, net, X, T, seed):
         """Adam in three phases of decreasing step size (lr, lr/5, lr/25)."""
         cfg = self.cfg
@@ -310,9 +316,10 @@ class Surrogate:
         the ensemble-mean peak equivalent plastic strain when ``with_ep``."""
         torch = _torch()
         X = torch.tensor(normalise(params), device="cuda")
+        v = self._speed(params)[:, None]
         peaks = []
         for net in self.nets:
-            A = net.predict(X) * self.y_std + self.y_mean
+            A = (net.predict(X) * self.y_std + self.y_mean) * v
             peaks.append(self._reconstruct_peak(A))
         P = torch.stack(peaks)
         mean = P.mean(dim=0)
@@ -334,7 +341,7 @@ class Surrogate:
         dist, idx = d.topk(k_nn, largest=False)
         w = 1.0 / dist.clamp_min(1e-6) ** 2
         w = w / w.sum(dim=1, keepdim=True)
-        A = (self.train_Y[idx] * w[..., None]).sum(dim=1)
+        A = (self.train_Y[idx] * w[..., None]).sum(dim=1) * self._speed(params)[:, None]
         if getattr(self, "with_ep", False):
             return self._reconstruct_peak(A), (self.train_ep[idx] * w).sum(dim=1)
         return self._reconstruct_peak(A)

@@ -98,8 +98,8 @@ def test_snapshots_match_final_state(cilib):
 def test_small_surrogate_end_to_end(cilib):
     pytest.importorskip("torch")
     from cppimpact_gb300 import surrogate as sg
-    cfg = sg.Config(n_cube=4, steps=400, every=50, rank=8, hidden=64, n_train=96, n_test=16,
-                    epochs=150, batch=32, ensemble=2)
+    cfg = sg.Config(n_cube=4, steps=400, every=50, rank=8, hidden=64, n_train=128, n_test=16,
+                    epochs=300, batch=32, ensemble=2)
     rng = np.random.default_rng(cfg.seed)
     ptr, pte = sg.sample_params(cfg.n_train, rng), sg.sample_params(cfg.n_test, rng)
     s_tr, _, _ = sg.generate(ptr, cfg)
