@@ -64,6 +64,12 @@ def workload(name: str):
     return m, setup, desc
 
 
+# DRAM bytes (read + write) per launch of the step kernel, from the ncu capture
+# summarised in profiles/k_step_qp10_shell_half.md (half shell, scaled x2 for the full
+# shell: elements and nodes double exactly).
+MEASURED_TRAFFIC = {"shell": 2 * 132.39e6, "shell_half": 132.39e6}
+
+
 def algorithmic_bytes(npe: int, E: int, N: int):
     """Per step: 4 npe + 56 nq per element + 112 per node (X0 fp32, u/v fp64 r/w, m fp32).
     The element kernel alone: connectivity + stress state r/w + X0, u, v reads."""
@@ -230,7 +236,9 @@ def run_ours(args, rank, world):
                            else "k_elem (element force + J2 + colour assembly)"),
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_src,
-                "traffic": args.traffic, "kernel_ms": round(k_elem_ms, 4),
+                "traffic": (args.traffic if args.traffic is not None
+                            else MEASURED_TRAFFIC.get(args.workload) if fused else None),
+                "kernel_ms": round(k_elem_ms, 4),
                 "other_kernel_ms_per_step": round(k_node_ms, 4),
                 "bytes_formula": "E(4 npe + 56 nq) + 112 N" if fused else "E(4 npe + 56 nq) + 60 N"}
     step_roof = {"achieved": round(step_bytes / (ms_step * 1e-3) / 1e9, 1),

@@ -107,7 +107,7 @@ EXPORTS = {
     "ci_batch_get_state": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _fp, _ubp,
                                      C.POINTER(C.c_longlong)]),
     "ci_batch_destroy": (C.c_int, [C.c_void_p]),
-    "ci_batch_tuning": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _fp]),
+    "ci_batch_tuning": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, _fp]),
     "ci_batch_run_snapshots": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, _fp]),
     "ci_batch_node_order": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip]),
     "ci_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
@@ -327,7 +327,7 @@ class Batch:
     wall_offset, wall_stiffness, vel, dt, t_end (and optionally pos)."""
 
     def __init__(self, instances, *, gravity=(0.0, 0.0, -9.81), device=0, chunk_nodes=0,
-                 block_threads=0, elem_lanes=0, autotune_steps=0):
+                 block_threads=0, elem_lanes=0, autotune_steps=0, chunk_elements=0):
         self._meshes = []
         arr = (CiInstance * len(instances))()
         shared = {}  # instances passing the same arrays share one copy (and one plan)
@@ -349,7 +349,7 @@ class Batch:
         opt = CiOptions()
         lib().ci_default_options(C.byref(opt))
         opt.gravity = (C.c_double * 3)(*gravity)
-        opt.device, opt.chunk_nodes = device, chunk_nodes
+        opt.device, opt.chunk_nodes, opt.chunk_elements = device, chunk_nodes, chunk_elements
         opt.block_threads, opt.elem_lanes = block_threads, elem_lanes
         opt.autotune_steps = autotune_steps
         self._arr = arr
@@ -359,11 +359,11 @@ class Batch:
 
     def tuning(self, npe) -> dict:
         """Tile shape of the group of npe-node elements (the autotuner's choice if tuned)."""
-        cn, bs, ln, ms = C.c_int(0), C.c_int(0), C.c_int(0), C.c_float(0)
-        check(lib().ci_batch_tuning(self._h, npe, C.byref(cn), C.byref(bs), C.byref(ln),
-                                    C.byref(ms)))
-        return dict(chunk_nodes=cn.value, block_threads=bs.value, elem_lanes=ln.value,
-                    trial_ms_per_step=ms.value)
+        ce, cn, bs, ln, ms = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0), C.c_float(0)
+        check(lib().ci_batch_tuning(self._h, npe, C.byref(ce), C.byref(cn), C.byref(bs),
+                                    C.byref(ln), C.byref(ms)))
+        return dict(chunk_elements=ce.value, chunk_nodes=cn.value, block_threads=bs.value,
+                    elem_lanes=ln.value, trial_ms_per_step=ms.value)
 
     def run(self) -> float:
         """Runs every instance to its end time; returns the batch's device time in ms."""

@@ -83,7 +83,7 @@ struct Group {
   long long S = 0, Lt = 0;
   int max_local = 0;
   size_t smem = 0;
-  int block_threads = 128, elem_lanes = 4, chunk_nodes = 896;
+  int block_threads = 128, elem_lanes = 4, chunk_nodes = 896, chunk_elements = 0;
   float tuned_ms_per_step = 0.f;  // autotuner's trial time of the chosen shape (0: not tuned)
   std::vector<int> insts;  // global instance ids
   int max_steps = 0;
@@ -270,7 +270,7 @@ int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& 
       const size_t j = uniq[i];
       const ci_instance& I = in[G.insts[j]];
       ok[j] = build_plan(I.mesh.num_nodes, I.mesh.num_elements, I.mesh.nodes_per_element,
-                         I.mesh.xloc, I.mesh.element_nodes, opt.chunk_elements, G.chunk_nodes, 304,
+                         I.mesh.xloc, I.mesh.element_nodes, G.chunk_elements, G.chunk_nodes, 304,
                          &built[j], &errs[j]);
     }
   };
@@ -510,17 +510,40 @@ int enqueue_run_graph(Group& G, int total, int per_graph) {
   return CI_OK;
 }
 
-// Project autotuner: time `steps` steps of every candidate tile shape -- local-node
-// budget per chunk (plan), CTA size, lanes per tet10 element -- on the group's own
-// instances from their initial state, and keep the fastest.  Options fixed by the
-// caller are not varied.  The group is left built with the winner (graph not captured).
+// Project autotuner: times `steps` steps of candidate tile shapes on the group's own
+// instances from their initial state and keeps the fastest.  Stage 1 picks the plan --
+// elements per chunk (each instance's own split, or chunks bounded by nodes only) and
+// local-node budget -- at the default CTA shape; stage 2 the CTA size and lanes per
+// tet10 element for that plan.  Options fixed by the caller are not varied.  The group
+// is left built with the winner (graph not captured).
+int trial_shape(Group& G, int graphs, cudaEvent_t e0, cudaEvent_t e1, float* ms_per_step) {
+  int rc;
+  if ((rc = capture_graph(G))) return rc;
+  if ((rc = enqueue_run(G, false))) return rc;
+  CB_CUDA(cudaGraphLaunch(G.graph, G.stream));  // warm-up: uploads the graph
+  CB_CUDA(cudaEventRecord(e0, G.stream));
+  for (int r = 0; r < graphs; r++) CB_CUDA(cudaGraphLaunch(G.graph, G.stream));
+  CB_CUDA(cudaEventRecord(e1, G.stream));
+  CB_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  CB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  unsigned int st = 0;
+  CB_CUDA(cudaMemcpy(&st, G.status.p, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st & ST_DEGENERATE) return fail(CI_ERR_DEGENERATE, "an element has det J <= 0");
+  if (st & ST_NONFINITE) return fail(CI_ERR_NONFINITE, "non-finite nodal state");
+  *ms_per_step = ms / (float)(graphs * kGraphSteps);
+  return CI_OK;
+}
+
 int autotune_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& opt) {
-  std::vector<int> cns = opt.chunk_nodes ? std::vector<int>{opt.chunk_nodes}
-                                         : std::vector<int>{512, 768, 896, 1024};
-  std::vector<int> bss = opt.block_threads ? std::vector<int>{opt.block_threads}
-                                           : std::vector<int>{64, 128, 256};
-  std::vector<int> lanes = (G.npe == 4 || opt.elem_lanes) ? std::vector<int>{G.elem_lanes}
-                                                          : std::vector<int>{1, 4};
+  const std::vector<int> ces = opt.chunk_elements ? std::vector<int>{opt.chunk_elements}
+                                                  : std::vector<int>{0, 4096};
+  const std::vector<int> cns = opt.chunk_nodes ? std::vector<int>{opt.chunk_nodes}
+                                               : std::vector<int>{512, 768, 896, 1024};
+  const std::vector<int> bss = opt.block_threads ? std::vector<int>{opt.block_threads}
+                                                 : std::vector<int>{64, 128, 256};
+  const std::vector<int> lanes = (G.npe == 4 || opt.elem_lanes) ? std::vector<int>{G.elem_lanes}
+                                                                : std::vector<int>{1, 4};
   const int graphs = std::max(1, (opt.autotune_steps + kGraphSteps - 1) / kGraphSteps);
   cudaEvent_t e0, e1;
   CB_CUDA(cudaEventCreate(&e0));
@@ -532,45 +555,43 @@ int autotune_group(ci_batch* b, Group& G, const ci_instance* in, const ci_option
       cudaEventDestroy(b);
     }
   } ev{e0, e1};
-  float best = 0.f;
-  int best_cn = cns[0], best_bs = bss[0], best_ln = lanes[0];
-  for (int cn : cns) {
-    G.chunk_nodes = cn;
-    int rc = build_group(b, G, in, opt);
-    if (rc) return rc;
-    for (int bs : bss)
-      for (int ln : lanes) {
-        G.block_threads = bs;
-        G.elem_lanes = ln;
-        if ((rc = capture_graph(G))) return rc;
-        if ((rc = enqueue_run(G, false))) return rc;
-        CB_CUDA(cudaGraphLaunch(G.graph, G.stream));  // warm-up: uploads the graph
-        CB_CUDA(cudaEventRecord(e0, G.stream));
-        for (int r = 0; r < graphs; r++) CB_CUDA(cudaGraphLaunch(G.graph, G.stream));
-        CB_CUDA(cudaEventRecord(e1, G.stream));
-        CB_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        CB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        unsigned int st = 0;
-        CB_CUDA(cudaMemcpy(&st, G.status.p, sizeof(st), cudaMemcpyDeviceToHost));
-        if (st & ST_DEGENERATE) return fail(CI_ERR_DEGENERATE, "an element has det J <= 0");
-        if (st & ST_NONFINITE) return fail(CI_ERR_NONFINITE, "non-finite nodal state");
-        ms /= (float)(graphs * kGraphSteps);
-        if (best == 0.f || ms < best) {
-          best = ms;
-          best_cn = cn;
-          best_bs = bs;
-          best_ln = ln;
-        }
+  int rc;
+  float best = 0.f, ms = 0.f;
+  int best_ce = ces[0], best_cn = cns[0];
+  for (int ce : ces)
+    for (int cn : cns) {
+      G.chunk_elements = ce;
+      G.chunk_nodes = cn;
+      if ((rc = build_group(b, G, in, opt))) return rc;
+      if ((rc = trial_shape(G, graphs, e0, e1, &ms))) return rc;
+      if (best == 0.f || ms < best) {
+        best = ms;
+        best_ce = ce;
+        best_cn = cn;
       }
+    }
+  if (G.chunk_elements != best_ce || G.chunk_nodes != best_cn) {
+    G.chunk_elements = best_ce;
+    G.chunk_nodes = best_cn;
+    if ((rc = build_group(b, G, in, opt))) return rc;
   }
+  const int bs0 = G.block_threads, ln0 = G.elem_lanes;
+  int best_bs = bs0, best_ln = ln0;
+  for (int bs : bss)
+    for (int ln : lanes) {
+      if (bs == bs0 && ln == ln0) continue;  // measured in stage 1
+      G.block_threads = bs;
+      G.elem_lanes = ln;
+      if ((rc = trial_shape(G, graphs, e0, e1, &ms))) return rc;
+      if (ms < best) {
+        best = ms;
+        best_bs = bs;
+        best_ln = ln;
+      }
+    }
   G.block_threads = best_bs;
   G.elem_lanes = best_ln;
   G.tuned_ms_per_step = best;
-  if (G.chunk_nodes != best_cn) {
-    G.chunk_nodes = best_cn;
-    return build_group(b, G, in, opt);
-  }
   return CI_OK;
 }
 
@@ -672,6 +693,7 @@ int ci_batch_create(const ci_instance* inst, int n, const ci_options* opt_in, ci
     G->block_threads = opt.block_threads ? opt.block_threads : 128;
     G->elem_lanes = opt.elem_lanes ? opt.elem_lanes : 4;
     G->chunk_nodes = opt.chunk_nodes ? opt.chunk_nodes : 896;
+    G->chunk_elements = opt.chunk_elements;
     if (G->block_threads != 64 && G->block_threads != 128 && G->block_threads != 256)
       return fail(CI_ERR_INVALID, "block_threads must be 64, 128 or 256");
     if (G->elem_lanes != 1 && G->elem_lanes != 4)
@@ -726,11 +748,12 @@ int ci_batch_run(ci_batch* b, float* device_ms) {
   return CI_OK;
 }
 
-int ci_batch_tuning(ci_batch* b, int npe, int* chunk_nodes, int* block_threads, int* elem_lanes,
-                    float* trial_ms_per_step) {
+int ci_batch_tuning(ci_batch* b, int npe, int* chunk_elements, int* chunk_nodes, int* block_threads,
+                    int* elem_lanes, float* trial_ms_per_step) {
   if (!b || (npe != 4 && npe != 10)) return fail(CI_ERR_INVALID, "ci_batch_tuning: bad arguments");
   const Group* G = b->g[npe == 4 ? 0 : 1].get();
   if (!G) return fail(CI_ERR_INVALID, "ci_batch_tuning: the batch has no instance of that type");
+  if (chunk_elements) *chunk_elements = G->chunk_elements;
   if (chunk_nodes) *chunk_nodes = G->chunk_nodes;
   if (block_threads) *block_threads = G->block_threads;
   if (elem_lanes) *elem_lanes = G->npe == 10 ? G->elem_lanes : 1;

@@ -123,18 +123,35 @@ def jacobi_eigh(A: np.ndarray, sweeps: int = 60, tol: float = 1e-14):
     return w[order], V[:, order]
 
 
-def generate(params: np.ndarray, cfg: Config, mesh: mg.TetMesh | None = None):
-    """Batched solves; returns (snapshots [n, snaps, 3N] FP32 torch in caller node order,
-    peak equivalent plastic strain [n], device ms)."""
-    torch = _torch()
-    mesh = mesh or mg.cube(cfg.n_cube, 1)
+def _instances(params, cfg, mesh):
     inst = []
     for v, sy, h, tilt in params:
         st = tilted_setup(mesh, v, tilt)
         st["t_end"] = (cfg.steps - 0.5) * st["dt"]
         inst.append(dict(xloc=mesh.xloc, conn=mesh.conn, E=E, nu=NU, rho=RHO, sigma_y0=sy,
                          H=h * E, **st))
-    b = api.Batch(inst)
+    return inst
+
+
+def tune_shape(params: np.ndarray, cfg: Config, mesh: mg.TetMesh | None = None,
+               steps: int = 64) -> dict:
+    """Tile shape the batch autotuner picks for a batch like `params` (timed on it)."""
+    mesh = mesh or mg.cube(cfg.n_cube, 1)
+    b = api.Batch(_instances(params, cfg, mesh), autotune_steps=steps)
+    t = b.tuning(mesh.npe)
+    b.close()
+    return {k: t[k] for k in ("chunk_elements", "chunk_nodes", "block_threads")}
+
+
+def generate(params: np.ndarray, cfg: Config, mesh: mg.TetMesh | None = None,
+             shape: dict | None = None):
+    """Batched solves (tile shape `shape`, e.g. from tune_shape; default plan otherwise);
+    returns (snapshots [n, snaps, 3N] FP32 torch in caller node order, peak equivalent
+    plastic strain [n], device ms)."""
+    torch = _torch()
+    mesh = mesh or mg.cube(cfg.n_cube, 1)
+    inst = _instances(params, cfg, mesh)
+    b = api.Batch(inst, **(shape or {}))
     n, N = len(inst), mesh.num_nodes
     snap = torch.zeros((cfg.snaps, n * N, 3), dtype=torch.float32, device="cuda")
     ms = b.run_snapshots(cfg.every, snap.data_ptr(), cfg.snaps)
@@ -347,12 +364,12 @@ class Surrogate:
         return self._reconstruct_peak(A)
 
 
-def fallback_runs(params: np.ndarray, cfg: Config, mesh=None):
+def fallback_runs(params: np.ndarray, cfg: Config, mesh=None, shape=None):
     """The solver for the given queries (one batch): peak displacement, peak equivalent
     plastic strain, device ms."""
     if len(params) == 0:
         return np.zeros(0), np.zeros(0), 0.0
-    s, ep, ms = generate(params, cfg, mesh)
+    s, ep, ms = generate(params, cfg, mesh, shape)
     return peak_disp(s).cpu().numpy(), ep, ms
 
 
@@ -407,11 +424,19 @@ def study(cfg: Config, plain_sample: int = 4, audit_fail_fraction: float = 0.1) 
     mesh = mg.cube(cfg.n_cube, 1)
     out = {"config": dataclasses.asdict(cfg), "mesh": {"elements": mesh.num_elements,
                                                        "nodes": mesh.num_nodes}}
+    # tile shapes for big batches (training and evaluation runs) and for fallback-sized
+    # ones, each picked by the autotuner on a batch of that size (one-off)
     t0 = time.perf_counter()
-    s_tr, ep_tr, ms_tr = generate(ptr, cfg, mesh)
+    n_fb = max(1, int(math.ceil((cfg.audit_fraction + 0.02) * cfg.n_test)))
+    shape_big = tune_shape(ptr[:min(len(ptr), 256)], cfg, mesh)
+    shape_fb = tune_shape(pte[:n_fb], cfg, mesh)
+    out["tuning"] = {"big": shape_big, "fallback": shape_fb, "fallback_batch": n_fb,
+                     "wall_s": time.perf_counter() - t0}
+    t0 = time.perf_counter()
+    s_tr, ep_tr, ms_tr = generate(ptr, cfg, mesh, shape_big)
     out["train_runs"] = {"wall_s": time.perf_counter() - t0, "device_ms": ms_tr}
     t0 = time.perf_counter()
-    s_te, ep_te, ms_te = generate(pte, cfg, mesh)
+    s_te, ep_te, ms_te = generate(pte, cfg, mesh, shape_big)
     wall_te = time.perf_counter() - t0
     truth_d, truth_ep = peak_disp(s_te).cpu().numpy(), np.asarray(ep_te)
     del s_te
@@ -438,7 +463,7 @@ def study(cfg: Config, plain_sample: int = 4, audit_fail_fraction: float = 0.1) 
     audit[arng.choice(cand, n_audit, replace=False)] = True
     rerun = flagged | audit
     t0 = time.perf_counter()
-    fb_d, fb_ep, fb_ms = fallback_runs(pte[rerun], cfg, mesh)
+    fb_d, fb_ep, fb_ms = fallback_runs(pte[rerun], cfg, mesh, shape_fb)
     t_fb = time.perf_counter() - t0
     final_d, final_ep = mean.copy(), ep_pred.copy()
     final_d[rerun], final_ep[rerun] = fb_d, fb_ep
@@ -449,7 +474,7 @@ def study(cfg: Config, plain_sample: int = 4, audit_fail_fraction: float = 0.1) 
     if full_fallback:
         rest = ~rerun
         t0 = time.perf_counter()
-        d2, e2, _ = fallback_runs(pte[rest], cfg, mesh)
+        d2, e2, _ = fallback_runs(pte[rest], cfg, mesh, shape_big)
         t_full = time.perf_counter() - t0
         final_d[rest], final_ep[rest] = d2, e2
     t_sur = t_pred + t_fb + t_full
@@ -476,7 +501,7 @@ def study(cfg: Config, plain_sample: int = 4, audit_fail_fraction: float = 0.1) 
                      "batched_sweep_wall_s": wall_te, "batched_sweep_device_ms": ms_te,
                      "plain_run_device_ms": plain_ms}
     rph = lambda count, sec: count / max(sec, 1e-12) * 3600.0
-    one_off = out["train_runs"]["wall_s"] + out["fit"]["wall_s"]
+    one_off = out["tuning"]["wall_s"] + out["train_runs"]["wall_s"] + out["fit"]["wall_s"]
     out["runs_per_hour"] = {
         "surrogate": rph(n, t_sur),
         "batched_solver": rph(n, wall_te),

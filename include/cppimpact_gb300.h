@@ -98,9 +98,9 @@ typedef struct ci_options {
   int block_threads;  /* threads per chunk CTA of the fused kernel: 64, 128 or 256; 0 = automatic */
   int elem_lanes;     /* tet10 fused kernel: 4 = one lane per Gauss point, 1 = one thread per
                          element; 0 = automatic (4) */
-  int autotune_steps; /* ci_batch_create only: > 0 = time this many steps of every candidate
-                         tile shape (chunk_nodes x block_threads x elem_lanes, those left 0
-                         above) and keep the fastest, see ci_batch_tuning; 0 = no tuning */
+  int autotune_steps; /* ci_batch_create only: > 0 = time this many steps of candidate tile
+                         shapes (chunk_elements, chunk_nodes, block_threads, elem_lanes: those
+                         left 0 above) and keep the fastest, see ci_batch_tuning; 0 = none */
 } ci_options;
 
 /* energy terms (FP64), see ci_get_energy */
@@ -198,11 +198,12 @@ int ci_batch_get_state(ci_batch* b, int i, double* x, double* v, float* epbar,
                        unsigned char* contact, long long* nsteps);
 int ci_batch_destroy(ci_batch* b);
 /* Tile shape the batch's group of `npe`-node elements runs with (after autotuning, the
- * winner; trial_ms_per_step its trial time, 0 when not tuned).  The shape changes the
- * plan and so the FP32 rounding of the results: to reproduce a tuned batch bit for bit,
- * pass the returned shape in ci_options (it then also equals the unbatched run). */
-int ci_batch_tuning(ci_batch* b, int npe, int* chunk_nodes, int* block_threads, int* elem_lanes,
-                    float* trial_ms_per_step);
+ * winner; trial_ms_per_step its trial time, 0 when not tuned); chunk_elements 0 means
+ * each instance's own automatic split.  The shape changes the plan and so the FP32
+ * rounding of the results: to reproduce a tuned batch bit for bit, pass the returned
+ * shape in ci_options (it then also equals the unbatched run with those options). */
+int ci_batch_tuning(ci_batch* b, int npe, int* chunk_elements, int* chunk_nodes, int* block_threads,
+                    int* elem_lanes, float* trial_ms_per_step);
 /* A run of a batch of one element type that also records the displacement of every
  * node every `every` steps (even) into d_snap [max_snaps][N_total][3] (device FP32,
  * plan order, instances concatenated); snapshot s is the state after (s+1)*every

@@ -68,14 +68,16 @@ def test_autotuned_batch(cilib):
     b.run()
     for npe in (4, 10):
         t = b.tuning(npe)
-        assert t["chunk_nodes"] in (512, 768, 1024)
+        assert t["chunk_elements"] in (0, 4096)
+        assert t["chunk_nodes"] in (512, 768, 896, 1024)
         assert t["block_threads"] in (64, 128, 256)
         assert t["elem_lanes"] in ((1,) if npe == 4 else (1, 4))
         assert t["trial_ms_per_step"] > 0
     for i, d in enumerate(inst):
         npe = d["conn"].shape[1]
         t = b.tuning(npe)
-        ss, n = _single(cilib, d, chunk_nodes=t["chunk_nodes"], block_threads=t["block_threads"],
+        ss, n = _single(cilib, d, chunk_elements=t["chunk_elements"], chunk_nodes=t["chunk_nodes"],
+                        block_threads=t["block_threads"],
                         elem_lanes=t["elem_lanes"] if npe == 10 else 0)
         bs = b.state(i)
         assert bs["nsteps"] == n
