@@ -95,7 +95,6 @@ struct Group {
   DBuf<int> lgid, lslot, slot_row, bnd, node_inst;
   DBuf<float> lx0, slot0, slot1, mass, d0f, acc, epbar, peak;
   DBuf<double> ua, va, ub, vb, v0, d0, work;
-  DBuf<float> ufa, vfa, ufb, vfb;  // FP32 copies of the state buffers
   DBuf<unsigned char> contact;
   DBuf<float4> sig_a;
   DBuf<float2> sig_b;
@@ -172,10 +171,6 @@ FusedArgs group_args(const Group& G, int i_in_graph) {
     F.v_cur[k] = (even ? G.va.p : G.vb.p) + k * N;
     F.u_prv[k] = (even ? G.ub.p : G.ua.p) + k * N;
     F.v_prv[k] = (even ? G.vb.p : G.va.p) + k * N;
-    F.uf_cur[k] = (even ? G.ufa.p : G.ufb.p) + k * N;
-    F.vf_cur[k] = (even ? G.vfa.p : G.vfb.p) + k * N;
-    F.uf_prv[k] = (even ? G.ufb.p : G.ufa.p) + k * N;
-    F.vf_prv[k] = (even ? G.vfb.p : G.vfa.p) + k * N;
     F.halo_cur[k] = (even ? G.slot0.p : G.slot1.p) + k * S;
     F.halo_prv[k] = (even ? G.slot1.p : G.slot0.p) + k * S;
     F.acc[k] = G.acc.p + k * N;
@@ -189,7 +184,7 @@ FusedArgs group_args(const Group& G, int i_in_graph) {
   F.epbar = G.epbar.p;
   F.chunk_work = G.work.p;
   F.status = G.status.p;
-  F.bnd_final = 0;
+  F.state_final = 0;
   F.store_acc = 0;
   F.inst_ep = G.inst_ep.p;
   F.inst_np = G.inst_np.p;
@@ -389,10 +384,6 @@ int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& 
   CB_CUDA(G.ua.alloc(3 * N));
   CB_CUDA(G.ub.alloc(3 * N));
   CB_CUDA(G.vb.alloc(3 * N));
-  CB_CUDA(G.ufa.alloc(3 * N));
-  CB_CUDA(G.vfa.alloc(3 * N));
-  CB_CUDA(G.ufb.alloc(3 * N));
-  CB_CUDA(G.vfb.alloc(3 * N));
   CB_CUDA(G.slot0.alloc(3 * (size_t)G.S));
   CB_CUDA(G.slot1.alloc(3 * (size_t)G.S));
   CB_CUDA(G.mass.alloc(N));
@@ -490,9 +481,6 @@ int enqueue_run(Group& G, bool launch = true) {
   np0.N = G.N;
   k_node_init<true><<<(G.N + 255) / 256, 256, 0, st>>>(A, np0, G.inst_np.p, G.node_inst.p,
                                                        G.d0f.p);
-  CB_CUDA(cudaGetLastError());
-  k_shadows<<<(unsigned)((3 * N + 255) / 256), 256, 0, st>>>(G.ua.p, G.va.p, G.ufa.p, G.vfa.p,
-                                                            3 * (long long)N);
   CB_CUDA(cudaGetLastError());
   if (launch) {
     // all global steps: max_steps + 1 (the last instance's boundary finalisation)
@@ -596,13 +584,11 @@ int autotune_group(ci_batch* b, Group& G, const ci_instance* in, const ci_option
 }
 
 // Displacement of every node after k = *step_ctr global steps, FP32, into
-// snap[(k / every - 1)][node][3] (plan order).  Interior nodes of an instance still
-// stepping hold S^k in buffer k & 1; its boundary nodes are completed from S^{k-1} and
-// the halo of step k-1 exactly as the next step would; instances that have finished
-// (k > nsteps) hold their final state in buffer nsteps & 1.
-__global__ void k_snapshot(FusedArgs A0, FusedArgs A1, const int* node_inst,
-                           const unsigned char* is_bnd, int N, int every, float* snap,
-                           int max_snaps) {
+// snap[(k / every - 1)][node][3] (plan order).  A node of an instance still stepping
+// is completed from S^{k-1} and the halo of step k-1 exactly as step k will do it;
+// instances that have finished (k > nsteps) hold their final state in buffer nsteps & 1.
+__global__ void k_snapshot(FusedArgs A0, FusedArgs A1, const int* node_inst, int N, int every,
+                           float* snap, int max_snaps) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
   const int k = *A0.step_ctr;
@@ -615,26 +601,13 @@ __global__ void k_snapshot(FusedArgs A0, FusedArgs A1, const int* node_inst,
   if (k > ns) {
     const FusedArgs& F = (ns & 1) ? A1 : A0;
     for (int c = 0; c < 3; c++) u[c] = F.u_cur[c][n];
-  } else if (!is_bnd[n]) {
-    const FusedArgs& F = (k & 1) ? A1 : A0;
-    for (int c = 0; c < 3; c++) u[c] = F.u_cur[c][n];
   } else {
-    // halo_prv of the step-k view is the halo of step k-1
+    // the step-k view: prv holds S^{k-1}, halo_prv the halo of step k-1
     const FusedArgs& F = (k & 1) ? A1 : A0;
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    for (int s = F.P.slot_row[n]; s < F.P.slot_row[n + 1]; s++) {
-      fx = __fadd_rn(fx, F.halo_prv[0][s]);
-      fy = __fadd_rn(fy, F.halo_prv[1][s]);
-      fz = __fadd_rn(fz, F.halo_prv[2][s]);
-    }
     double v[3];
-    for (int c = 0; c < 3; c++) {
-      u[c] = F.u_prv[c][n];
-      v[c] = F.v_prv[c][n];
-    }
     float a[3], uf[3], vf[3];
     bool hit;
-    node_step(F.inst_np[inst], fx, fy, fz, F.mass[n], F.d0f[n], F.d0, n, u, v, a, hit, uf, vf);
+    complete_node(F, F.inst_np[inst], n, u, v, a, hit, uf, vf);
   }
   float* o = snap + ((size_t)si * N + n) * 3;
   o[0] = (float)u[0];
@@ -809,14 +782,6 @@ int ci_batch_run_snapshots(ci_batch* b, int every, float* d_snap, int max_snaps,
   // graph: `every` steps, then the snapshot of the state after them, then the tick
   if (G.graph) cudaGraphExecDestroy(G.graph);
   G.graph = nullptr;
-  std::vector<unsigned char> isb(G.N, 0);
-  {
-    std::vector<int> sr(G.N + 1);
-    CB_CUDA(cudaMemcpy(sr.data(), G.slot_row.p, sizeof(int) * (G.N + 1), cudaMemcpyDeviceToHost));
-    for (int n = 0; n < G.N; n++) isb[n] = sr[n + 1] - sr[n] > 1;
-  }
-  DBuf<unsigned char> d_isb;
-  CB_CUDA(d_isb.upload(isb, G.stream));
   cudaGraph_t g = nullptr;
   CB_CUDA(cudaStreamBeginCapture(G.stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
@@ -827,8 +792,7 @@ int ci_batch_run_snapshots(ci_batch* b, int every, float* d_snap, int max_snaps,
   if (err == cudaSuccess) {
     k_tick<<<1, 1, 0, G.stream>>>(G.step_ctr.p, every);
     k_snapshot<<<(G.N + 255) / 256, 256, 0, G.stream>>>(group_args(G, 0), group_args(G, 1),
-                                                        G.node_inst.p, d_isb.p, G.N, every, d_snap,
-                                                        max_snaps);
+                                                        G.node_inst.p, G.N, every, d_snap, max_snaps);
     err = cudaGetLastError();
   }
   cudaError_t e2 = cudaStreamEndCapture(G.stream, &g);

@@ -462,15 +462,15 @@ __global__ void __launch_bounds__(256) k_node(NodeArrays A, NodeParams p) {
 // ---------------------------------------------------------------------------
 // Fused step (one launch per time step, no grid-wide barrier).
 //
-// Node state S^n = (u^n, v^{n+1/2}) is double-buffered.  A chunk's INTERIOR nodes are
-// touched by no other chunk: the chunk updates them in its epilogue, S^n -> S^{n+1}
-// written to the other buffer.  BOUNDARY nodes are touched by several chunks: each
-// chunk writes its partial force to the node's slot in the halo buffer of step n,
-// and at the start of step n+1 every chunk touching the node sums the slots (fixed
-// chunk order) and applies the same update to S^n itself; the owner stores the
-// result.  The update uses explicitly rounded operations so every chunk obtains the
-// same bits.  After the last step of a call k_finalize_boundary completes S^N for the
-// boundary nodes.
+// Node state S^n = (u^n, v^{n+1/2}) is double-buffered: step n reads S^{n-1} from one
+// buffer and its owner writes S^n to the other.  Every chunk writes its partial force
+// on each of its local nodes to that node's slot in the halo buffer of step n.  At the
+// start of step n+1 every chunk touching a node sums the node's slots in fixed chunk
+// order and applies the central-difference update to S^n itself (an interior node has
+// one slot and one chunk; a boundary node is updated identically by every chunk that
+// touches it); the owner stores S^{n+1}.  The update uses explicitly rounded
+// operations, so every chunk obtains the same bits.  After the last step of a call
+// k_finalize_nodes completes S^N.
 // ---------------------------------------------------------------------------
 struct FusedArgs {
   DevPlan P;
@@ -478,12 +478,6 @@ struct FusedArgs {
   double* v_cur[3];
   double* u_prv[3];
   double* v_prv[3];
-  // FP32 copies of u and v, double-buffered with them: staging reads these, so the
-  // FP64 state is converted once per update instead of at every staging
-  float* uf_cur[3];
-  float* vf_cur[3];
-  float* uf_prv[3];
-  float* vf_prv[3];
   const float* halo_prv[3];
   float* halo_cur[3];
   const float* mass;
@@ -496,11 +490,11 @@ struct FusedArgs {
   float* epbar;
   double* chunk_work;
   unsigned int* status;
-  int bnd_final;  // boundary nodes already hold S^n in the cur buffer
+  int state_final;  // every node already holds S^n in the cur buffer (first step of a call)
   int store_acc;
   // batched solves (k_step<..., BATCH = true>): per-instance parameters and step counts;
   // the global step is *step_ctr + step_off.  An instance steps while step < nsteps,
-  // finalises its boundary nodes at step == nsteps and idles afterwards.
+  // completes its nodes at step == nsteps and idles afterwards.
   const ElemParams* inst_ep;
   const NodeParams* inst_np;
   const int* inst_nsteps;
@@ -512,8 +506,8 @@ struct FusedArgs {
 struct ChunkStep {
   ElemParams ep;
   NodeParams np;
-  int bnd_final;
-  int mode;  // 0 step, 1 finalise boundary nodes only, 2 idle
+  int state_final;
+  int mode;  // 0 step, 1 complete the nodes only, 2 idle
 };
 
 template <bool BATCH>
@@ -523,7 +517,7 @@ __device__ __forceinline__ ChunkStep chunk_step(const FusedArgs& A, const ChunkI
   if (!BATCH) {
     c.ep = ep;
     c.np = np;
-    c.bnd_final = A.bnd_final;
+    c.state_final = A.state_final;
     c.mode = 0;
     return c;
   }
@@ -531,7 +525,7 @@ __device__ __forceinline__ ChunkStep chunk_step(const FusedArgs& A, const ChunkI
   const int n = A.inst_nsteps[ch.inst];
   c.ep = A.inst_ep[ch.inst];
   c.np = A.inst_np[ch.inst];
-  c.bnd_final = k == 0;
+  c.state_final = k == 0;
   c.mode = k < n ? 0 : (k == n ? 1 : 2);
   return c;
 }
@@ -587,18 +581,14 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
 }
 
 __device__ __forceinline__ void store_node(const FusedArgs& A, double* const (&uo)[3],
-                                           double* const (&vo)[3], float* const (&ufo)[3],
-                                           float* const (&vfo)[3], int g, const double (&u)[3],
-                                           const double (&v)[3], const float (&uf)[3],
-                                           const float (&vf)[3], const float (&a)[3],
-                                           bool in_contact, bool store_acc) {
+                                           double* const (&vo)[3], int g, const double (&u)[3],
+                                           const double (&v)[3], const float (&vf)[3],
+                                           const float (&a)[3], bool in_contact, bool store_acc) {
   bool finite = true;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     uo[k][g] = u[k];
     vo[k][g] = v[k];
-    ufo[k][g] = uf[k];
-    vfo[k][g] = vf[k];
     finite = finite && isfinite(vf[k]);
     if (store_acc) A.acc[k][g] = a[k];
   }
@@ -606,6 +596,27 @@ __device__ __forceinline__ void store_node(const FusedArgs& A, double* const (&u
   const unsigned char old = A.contact[g];
   const unsigned char flag = in_contact ? 3 : (old & 2);
   if (flag != old) A.contact[g] = flag;
+}
+
+// S^n of node g from S^{n-1} (prv buffer) and the halo of step n-1: the sum of its
+// slots in fixed order, then the update.  Every chunk touching g computes the same bits.
+__device__ __forceinline__ void complete_node(const FusedArgs& A, const NodeParams& np, int g,
+                                              double (&u)[3], double (&v)[3], float (&a)[3],
+                                              bool& hit, float (&uf)[3], float (&vf)[3]) {
+  const DevPlan& P = A.P;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  const int s1 = P.slot_row[g + 1];
+  for (int s = P.slot_row[g]; s < s1; s++) {
+    fx = __fadd_rn(fx, A.halo_prv[0][s]);
+    fy = __fadd_rn(fy, A.halo_prv[1][s]);
+    fz = __fadd_rn(fz, A.halo_prv[2][s]);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    u[k] = A.u_prv[k][g];
+    v[k] = A.v_prv[k][g];
+  }
+  node_step(np, fx, fy, fz, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit, uf, vf);
 }
 
 // Shared-memory node records of the fused kernels: p0 = (x, y, z, du_x),
@@ -625,48 +636,33 @@ __device__ __forceinline__ Tile make_tile(float* sm, int L) {
 }
 
 // Stage S^n of every local node of the chunk in shared memory (x relative to the
-// chunk origin, dt v), bringing boundary nodes from S^{n-1} to S^n first.
+// chunk origin, dt v): completed from S^{n-1} and the previous halo (the owner stores
+// it), or read as it is on the first step of a call.
 template <int BS>
 __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams& ep,
                                             const NodeParams& np, const ChunkInfo& ch,
-                                            int bnd_final, const Tile& T) {
+                                            int state_final, const Tile& T) {
   const DevPlan& P = A.P;
   const int L = ch.n_local;
-  // interior nodes: contiguous owned range, FP32 copies, independent loads
-  const int n_direct = bnd_final ? L : ch.n_int;
-#pragma unroll 4
-  for (int l = threadIdx.x; l < n_direct; l += BS) {
-    const int lb = ch.local_begin + l;
-    const int g = l < ch.n_int ? ch.own_begin + l : P.local_gid[lb];
-    const float ux = A.uf_cur[0][g], uy = A.uf_cur[1][g], uz = A.uf_cur[2][g];
-    const float vx = A.vf_cur[0][g], vy = A.vf_cur[1][g], vz = A.vf_cur[2][g];
-    T.p0[l] = make_float4(P.local_x0[lb] + ux, P.local_x0[(size_t)P.Lt + lb] + uy,
-                          P.local_x0[2 * (size_t)P.Lt + lb] + uz, ep.dt * vx);
-    T.p1[l] = make_float2(ep.dt * vy, ep.dt * vz);
-    T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  // boundary nodes: sum the previous step's partial forces and apply the update
 #pragma unroll 2
-  for (int l = n_direct + threadIdx.x; l < L; l += BS) {
+  for (int l = threadIdx.x; l < L; l += BS) {
     const int lb = ch.local_begin + l;
-    const int g = P.local_gid[lb];
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    const int s1 = P.slot_row[g + 1];
-    for (int s = P.slot_row[g]; s < s1; s++) {
-      fx = __fadd_rn(fx, A.halo_prv[0][s]);
-      fy = __fadd_rn(fy, A.halo_prv[1][s]);
-      fz = __fadd_rn(fz, A.halo_prv[2][s]);
-    }
-    double u[3], v[3];
+    const bool own = l < ch.n_own;
+    const int g = own ? ch.own_begin + l : P.local_gid[lb];
+    float uf[3], vf[3];
+    if (state_final) {
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-      u[k] = A.u_prv[k][g];
-      v[k] = A.v_prv[k][g];
+      for (int k = 0; k < 3; k++) {
+        uf[k] = (float)A.u_cur[k][g];
+        vf[k] = (float)A.v_cur[k][g];
+      }
+    } else {
+      double u[3], v[3];
+      float a[3];
+      bool hit;
+      complete_node(A, np, g, u, v, a, hit, uf, vf);
+      if (own) store_node(A, A.u_cur, A.v_cur, g, u, v, vf, a, hit, false);
     }
-    float a[3], uf[3], vf[3];
-    bool hit;
-    node_step(np, fx, fy, fz, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit, uf, vf);
-    if (l < ch.n_own) store_node(A, A.u_cur, A.v_cur, A.uf_cur, A.vf_cur, g, u, v, uf, vf, a, hit, false);
     T.p0[l] = make_float4(P.local_x0[lb] + uf[0], P.local_x0[(size_t)P.Lt + lb] + uf[1],
                           P.local_x0[2 * (size_t)P.Lt + lb] + uf[2], ep.dt * vf[0]);
     T.p1[l] = make_float2(ep.dt * vf[1], ep.dt * vf[2]);
@@ -674,34 +670,19 @@ __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams
   }
 }
 
-// Interior nodes S^n -> S^{n+1} (other buffer); boundary partial forces to the halo.
+// Every local node's partial force of this step to its slot in the halo.
 template <int BS>
-__device__ __forceinline__ void node_epilogue(const FusedArgs& A, const NodeParams& np,
-                                              const ChunkInfo& ch, const Tile& T) {
+__device__ __forceinline__ void node_epilogue(const FusedArgs& A, const ChunkInfo& ch,
+                                              const Tile& T) {
   const DevPlan& P = A.P;
   const int L = ch.n_local;
-#pragma unroll 2
+#pragma unroll 4
   for (int l = threadIdx.x; l < L; l += BS) {
     const float4 f = T.acc[l];
-    if (l < ch.n_int) {
-      const int g = ch.own_begin + l;
-      double u[3], v[3];
-      float a[3], uf[3], vf[3];
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        u[k] = A.u_cur[k][g];
-        v[k] = A.v_cur[k][g];
-      }
-      bool hit;
-      node_step(np, f.x, f.y, f.z, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit, uf, vf);
-      store_node(A, A.u_prv, A.v_prv, A.uf_prv, A.vf_prv, g, u, v, uf, vf, a, hit,
-                 A.store_acc != 0);
-    } else {
-      const int s = P.local_slot[ch.local_begin + l];
-      A.halo_cur[0][s] = f.x;
-      A.halo_cur[1][s] = f.y;
-      A.halo_cur[2][s] = f.z;
-    }
+    const int s = P.local_slot[ch.local_begin + l];
+    A.halo_cur[0][s] = f.x;
+    A.halo_cur[1][s] = f.y;
+    A.halo_cur[2][s] = f.z;
   }
 }
 
@@ -730,7 +711,7 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, Nod
   const Tile T = make_tile(sm, L);
   __shared__ float red[BS / 32];
 
-  stage_nodes<BS>(A, ep, np, ch, cs.bnd_final, T);
+  stage_nodes<BS>(A, ep, np, ch, cs.state_final, T);
   if (cs.mode == 1) return;
   __syncthreads();
 
@@ -781,7 +762,7 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, Nod
     }
   }
   __syncthreads();
-  node_epilogue<BS>(A, np, ch, T);
+  node_epilogue<BS>(A, ch, T);
   if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
 }
 
@@ -908,7 +889,7 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
   const Tile T = make_tile(sm, L);
   __shared__ float red[BS / 32];
 
-  stage_nodes<BS>(A, ep, np, ch, cs.bnd_final, T);
+  stage_nodes<BS>(A, ep, np, ch, cs.state_final, T);
   if (cs.mode == 1) return;
   __syncthreads();
 
@@ -1039,34 +1020,20 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
     }
   }
   __syncthreads();
-  node_epilogue<BS>(A, np, ch, T);
+  node_epilogue<BS>(A, ch, T);
   if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
 }
 
-// S^N of the boundary nodes after the last fused step of a call: reads S^{N-1} from
-// the prv buffer and the halo of step N-1, writes S^N (and a^N) to the cur buffer.
-static __global__ void __launch_bounds__(256) k_finalize_boundary(FusedArgs A, NodeParams np,
-                                                           const int* bnd_nodes, int nb) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nb) return;
-  const int g = bnd_nodes[i];
-  float fx = 0.f, fy = 0.f, fz = 0.f;
-  const int s1 = A.P.slot_row[g + 1];
-  for (int s = A.P.slot_row[g]; s < s1; s++) {
-    fx = __fadd_rn(fx, A.halo_prv[0][s]);
-    fy = __fadd_rn(fy, A.halo_prv[1][s]);
-    fz = __fadd_rn(fz, A.halo_prv[2][s]);
-  }
+// S^N of every node after the last fused step of a call: reads S^{N-1} from the prv
+// buffer and the halo of step N-1, writes S^N (and a^N) to the cur buffer.
+static __global__ void __launch_bounds__(256) k_finalize_nodes(FusedArgs A, NodeParams np) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= A.P.N) return;
   double u[3], v[3];
   float a[3], uf[3], vf[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    u[k] = A.u_prv[k][g];
-    v[k] = A.v_prv[k][g];
-  }
   bool hit;
-  node_step(np, fx, fy, fz, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit, uf, vf);
-  store_node(A, A.u_cur, A.v_cur, A.uf_cur, A.vf_cur, g, u, v, uf, vf, a, hit, true);
+  complete_node(A, np, g, u, v, a, hit, uf, vf);
+  store_node(A, A.u_cur, A.v_cur, g, u, v, vf, a, hit, A.store_acc != 0);
 }
 
 // a0 from zero internal force (wall at the start positions, gravity) and the half step
@@ -1111,14 +1078,6 @@ __global__ void __launch_bounds__(256) k_node_init(NodeArrays A, NodeParams p_ar
   }
   A.contact[n] = flag;
   if (!finite) atomicOr(A.status, (unsigned)ST_NONFINITE);
-}
-
-// FP32 copies of the FP64 state (after it was written by an initial condition).
-static __global__ void k_shadows(const double* u, const double* v, float* uf, float* vf, long long n3) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= n3) return;
-  uf[i] = st_f32(u[i]);
-  vf[i] = st_f32(v[i]);
 }
 
 // Adds n to the batched step counter (after each captured block of steps).

@@ -97,10 +97,7 @@ struct ci_solver {
   // path's second buffer)
   DBuf<double> d_u, d_v;   // [3][N]
   DBuf<double> d_ub, d_vb; // [3][N]
-  DBuf<float> d_ufa, d_vfa, d_ufb, d_vfb;  // FP32 copies of u, v (A and B buffers)
   DBuf<float> d_halo1;     // [3][S] second halo buffer of the fused path
-  DBuf<int> d_bnd;         // boundary nodes (plan ids)
-  int n_bnd = 0;
   DBuf<float> d_slot;      // [3][S]
   DBuf<float> d_mass;      // [N]
   DBuf<double> d_d0;       // [N]
@@ -178,7 +175,7 @@ struct ci_solver {
     A.status = d_status.p;
     return A;
   }
-  ci::FusedArgs fused_args(bool cur_is_a, int halo_cur, bool bnd_final, bool store_acc) const {
+  ci::FusedArgs fused_args(bool cur_is_a, int halo_cur, bool state_final, bool store_acc) const {
     ci::FusedArgs F;
     F.P = dev_plan();
     double* ua = d_u.p;
@@ -191,10 +188,6 @@ struct ci_solver {
       F.v_cur[k] = (cur_is_a ? va : vb) + (size_t)k * N;
       F.u_prv[k] = (cur_is_a ? ub : ua) + (size_t)k * N;
       F.v_prv[k] = (cur_is_a ? vb : va) + (size_t)k * N;
-      F.uf_cur[k] = (cur_is_a ? d_ufa.p : d_ufb.p) + (size_t)k * N;
-      F.vf_cur[k] = (cur_is_a ? d_vfa.p : d_vfb.p) + (size_t)k * N;
-      F.uf_prv[k] = (cur_is_a ? d_ufb.p : d_ufa.p) + (size_t)k * N;
-      F.vf_prv[k] = (cur_is_a ? d_vfb.p : d_vfa.p) + (size_t)k * N;
       F.halo_cur[k] = h[halo_cur] + (size_t)k * S;
       F.halo_prv[k] = h[halo_cur ^ 1] + (size_t)k * S;
       F.acc[k] = d_acc.p + (size_t)k * N;
@@ -208,7 +201,7 @@ struct ci_solver {
     F.epbar = d_epbar.p;
     F.chunk_work = d_work.p;
     F.status = d_status.p;
-    F.bnd_final = bnd_final ? 1 : 0;
+    F.state_final = state_final ? 1 : 0;
     F.store_acc = store_acc ? 1 : 0;
     F.inst_ep = nullptr;
     F.inst_np = nullptr;
@@ -310,29 +303,25 @@ cudaError_t launch_fused(ci_solver* s, const ci::FusedArgs& F) {
 }
 
 cudaError_t launch_finalize(ci_solver* s, const ci::FusedArgs& F) {
-  if (s->n_bnd == 0) return cudaSuccess;
-  ci::k_finalize_boundary<<<(s->n_bnd + 255) / 256, 256, 0, s->stream>>>(F, s->node_params(),
-                                                                         s->d_bnd.p, s->n_bnd);
+  ci::k_finalize_nodes<<<(s->N + 255) / 256, 256, 0, s->stream>>>(F, s->node_params());
   return cudaGetLastError();
 }
 
 // n fused steps from the state in buffer A, ending with the state in buffer A.
-cudaError_t enqueue_fused(ci_solver* s, int n, bool store_acc_last) {
+cudaError_t enqueue_fused(ci_solver* s, int n) {
   if (n <= 0) return cudaSuccess;
   cudaError_t e;
   for (int i = 0; i < n; i++) {
-    const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0, store_acc_last && i == n - 1);
+    const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0, false);
     if ((e = launch_fused(s, F))) return e;
   }
-  // boundary nodes: S^n from S^{n-1} (prv) and the halo of step n-1
+  // S^n from S^{n-1} (prv) and the halo of step n-1 (with the accelerations a^n)
   const ci::FusedArgs F = s->fused_args((n & 1) == 0, n & 1, false, true);
   if ((e = launch_finalize(s, F))) return e;
   if (n & 1) {
-    const size_t b = sizeof(double) * 3 * (size_t)s->N, bf = sizeof(float) * 3 * (size_t)s->N;
+    const size_t b = sizeof(double) * 3 * (size_t)s->N;
     if ((e = cudaMemcpyAsync(s->d_u.p, s->d_ub.p, b, cudaMemcpyDeviceToDevice, s->stream))) return e;
     if ((e = cudaMemcpyAsync(s->d_v.p, s->d_vb.p, b, cudaMemcpyDeviceToDevice, s->stream))) return e;
-    if ((e = cudaMemcpyAsync(s->d_ufa.p, s->d_ufb.p, bf, cudaMemcpyDeviceToDevice, s->stream))) return e;
-    if ((e = cudaMemcpyAsync(s->d_vfa.p, s->d_vfb.p, bf, cudaMemcpyDeviceToDevice, s->stream))) return e;
   }
   return cudaSuccess;
 }
@@ -368,15 +357,6 @@ cudaError_t enqueue_step(ci_solver* s, bool store_acc) {
     ci::k_node<false, true><<<nb, 256, 0, s->stream>>>(s->node_arrays(), s->node_params());
   else
     ci::k_node<false, false><<<nb, 256, 0, s->stream>>>(s->node_arrays(), s->node_params());
-  return cudaGetLastError();
-}
-
-// FP32 copies of the A-buffer state (fused path), after the FP64 state was written.
-cudaError_t refresh_shadows(ci_solver* s) {
-  if (!s->d_ufa.p) return cudaSuccess;
-  const long long n3 = 3 * (long long)s->N;
-  ci::k_shadows<<<(unsigned)((n3 + 255) / 256), 256, 0, s->stream>>>(s->d_u.p, s->d_v.p, s->d_ufa.p,
-                                                                   s->d_vfa.p, n3);
   return cudaGetLastError();
 }
 
@@ -481,7 +461,7 @@ int build_graph(ci_solver* s, int steps) {
   CI_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
   if (fused_path(s))
-    err = enqueue_fused(s, steps, false);
+    err = enqueue_fused(s, steps);
   else
     for (int i = 0; i < steps && err == cudaSuccess; i++) err = enqueue_step(s, false);
   cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
@@ -511,7 +491,7 @@ int enqueue_steps(ci_solver* s, int n) {
         rest -= G;
       }
     }
-    CI_CUDA(enqueue_fused(s, rest, true));
+    CI_CUDA(enqueue_fused(s, rest));
     s->steps_done += n;
     return CI_OK;
   }
@@ -635,16 +615,7 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   if (s->opt.step_kernel == 0) {
     CI_CUDA(s->d_ub.alloc(3 * N));
     CI_CUDA(s->d_vb.alloc(3 * N));
-    CI_CUDA(s->d_ufa.alloc(3 * N));
-    CI_CUDA(s->d_vfa.alloc(3 * N));
-    CI_CUDA(s->d_ufb.alloc(3 * N));
-    CI_CUDA(s->d_vfb.alloc(3 * N));
     CI_CUDA(s->d_halo1.alloc(3 * (size_t)s->S));
-    std::vector<int> bnd;
-    for (int n = 0; n < s->N; n++)
-      if (P.slot_row[n + 1] - P.slot_row[n] > 1) bnd.push_back(n);
-    s->n_bnd = (int)bnd.size();
-    if ((rc = upload(s->d_bnd, bnd, s->stream))) return rc;
   }
   CI_CUDA(s->d_mass.alloc(N));
   CI_CUDA(s->d_d0.alloc(N));
@@ -699,7 +670,6 @@ int ci_start(ci_solver* s, double dt) {
   ci::k_node_init<false><<<(s->N + 255) / 256, 256, 0, s->stream>>>(
       s->node_arrays(), s->node_params(), nullptr, nullptr, s->d_d0f.p);
   CI_CUDA(cudaGetLastError());
-  CI_CUDA(refresh_shadows(s));
   s->started = true;
   return check_status(s);
 }
@@ -817,7 +787,6 @@ int ci_set_state(ci_solver* s, const double* x, const double* v) {
                           s->stream));
   CI_CUDA(cudaMemcpyAsync(s->d_v.p, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice,
                           s->stream));
-  CI_CUDA(refresh_shadows(s));
   CI_CUDA(cudaStreamSynchronize(s->stream));
   return CI_OK;
 }
@@ -1042,7 +1011,7 @@ int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms) {
   if (fused_path(s)) {
     // out[0]: mean k_step duration; out[1]: the end-of-call boundary finalise
     for (int i = 0; i < nsteps; i++) {
-      const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0, i == nsteps - 1);
+      const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0, false);
       CI_CUDA(cudaEventRecord(ev[3 * i], s->stream));
       CI_CUDA(launch_fused(s, F));
       CI_CUDA(cudaEventRecord(ev[3 * i + 1], s->stream));
@@ -1051,11 +1020,9 @@ int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms) {
     CI_CUDA(launch_finalize(s, F));
     CI_CUDA(cudaEventRecord(ev[2], s->stream));
     if (nsteps & 1) {
-      const size_t b = sizeof(double) * 3 * (size_t)s->N, bf = sizeof(float) * 3 * (size_t)s->N;
+      const size_t b = sizeof(double) * 3 * (size_t)s->N;
       CI_CUDA(cudaMemcpyAsync(s->d_u.p, s->d_ub.p, b, cudaMemcpyDeviceToDevice, s->stream));
       CI_CUDA(cudaMemcpyAsync(s->d_v.p, s->d_vb.p, b, cudaMemcpyDeviceToDevice, s->stream));
-      CI_CUDA(cudaMemcpyAsync(s->d_ufa.p, s->d_ufb.p, bf, cudaMemcpyDeviceToDevice, s->stream));
-      CI_CUDA(cudaMemcpyAsync(s->d_vfa.p, s->d_vfb.p, bf, cudaMemcpyDeviceToDevice, s->stream));
     }
     CI_CUDA(cudaStreamSynchronize(s->stream));
     for (int i = 0; i < nsteps; i++) {

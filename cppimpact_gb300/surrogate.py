@@ -494,6 +494,13 @@ def study(cfg: Config, plain_sample: int = 4, audit_fail_fraction: float = 0.1) 
     }
     out["audit"] = {"flagged_by_spread": int(flagged.sum()), "audited": int(n_audit),
                     "rerun": int(rerun.sum()), "full_fallback": full_fallback}
+    # how the spread threshold trades re-runs against the error left in the answers
+    err_only = np.abs(mean - truth_d) / truth_d
+    out["spread_threshold_scan"] = [
+        {"threshold": th, "flagged": int((spread > th).sum()),
+         "unflagged_frac_over_2pct": float((err_only[spread <= th] > 0.02).mean()) if (spread <= th).any() else 0.0,
+         "unflagged_max": float(err_only[spread <= th].max()) if (spread <= th).any() else 0.0}
+        for th in (0.0025, 0.005, 0.01, 0.02)]
     plain = plain_run_ms(pte[:plain_sample], cfg, mesh)
     plain_ms = float(np.mean(plain))
     out["timing"] = {"predict_s": t_pred, "fallback_wall_s": t_fb, "fallback_device_ms": fb_ms,
