@@ -92,7 +92,7 @@ struct Group {
   DBuf<ChunkInfo> chunks;
   DBuf<uint16_t> conn;
   DBuf<uint8_t> color;
-  DBuf<int> lgid, lslot, slot_row, bnd, node_inst;
+  DBuf<int> lgid, lslot, lsrow, slot_row, bnd, node_inst;
   DBuf<float> lx0, slot0, slot1, mass, d0f, acc, epbar, peak;
   DBuf<double> ua, va, ub, vb, v0, d0, work;
   DBuf<unsigned char> contact;
@@ -159,6 +159,7 @@ FusedArgs group_args(const Group& G, int i_in_graph) {
   F.P.color = G.color.p;
   F.P.local_gid = G.lgid.p;
   F.P.local_slot = G.lslot.p;
+  F.P.local_srow = reinterpret_cast<const int2*>(G.lsrow.p);
   F.P.local_x0 = G.lx0.p;
   F.P.slot_row = G.slot_row.p;
   F.P.E = G.E;
@@ -302,7 +303,7 @@ int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& 
   std::vector<ChunkInfo> chunks;
   std::vector<uint16_t> conn((size_t)npe * G.E);
   std::vector<uint8_t> color;
-  std::vector<int> lgid, lslot, slot_row, bnd, node_inst;
+  std::vector<int> lgid, lslot, lsrow, slot_row, bnd, node_inst;
   std::vector<float> lx0(3 * (size_t)G.Lt), d0f;
   std::vector<double> d0, v0(3 * (size_t)G.N);
   std::vector<ElemParams> eps;
@@ -319,6 +320,7 @@ int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& 
       c.elem_end += T.elem_off;
       c.own_begin += T.node_off;
       c.local_begin += (int)l_off;
+      c.slot_begin += (int)s_off;
       c.inst = (int)j;
       chunks.push_back(c);
     }
@@ -329,6 +331,8 @@ int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& 
     for (size_t l = 0; l < P.local_gid.size(); l++) {
       lgid.push_back(P.local_gid[l] + T.node_off);
       lslot.push_back(P.local_slot[l] + (int)s_off);
+      lsrow.push_back(P.local_srow[2 * l] + (int)s_off);
+      lsrow.push_back(P.local_srow[2 * l + 1] + (int)s_off);
     }
     for (int n = 0; n < P.N; n++) {
       slot_row.push_back(P.slot_row[n] + (int)s_off);
@@ -369,6 +373,7 @@ int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& 
   CB_CUDA(G.color.upload(color, st));
   CB_CUDA(G.lgid.upload(lgid, st));
   CB_CUDA(G.lslot.upload(lslot, st));
+  CB_CUDA(G.lsrow.upload(lsrow, st));
   CB_CUDA(G.slot_row.upload(slot_row, st));
   CB_CUDA(G.bnd.upload(bnd, st));
   CB_CUDA(G.node_inst.upload(node_inst, st));
@@ -445,6 +450,7 @@ int enqueue_run(Group& G, bool launch = true) {
   P.color = G.color.p;
   P.local_gid = G.lgid.p;
   P.local_slot = G.lslot.p;
+  P.local_srow = reinterpret_cast<const int2*>(G.lsrow.p);
   P.local_x0 = G.lx0.p;
   P.slot_row = G.slot_row.p;
   P.E = G.E;
@@ -607,7 +613,8 @@ __global__ void k_snapshot(FusedArgs A0, FusedArgs A1, const int* node_inst, int
     double v[3];
     float a[3], uf[3], vf[3];
     bool hit;
-    complete_node(F, F.inst_np[inst], n, u, v, a, hit, uf, vf);
+    complete_node(F, F.inst_np[inst], n, F.P.slot_row[n], F.P.slot_row[n + 1], u, v, a, hit, uf,
+                  vf);
   }
   float* o = snap + ((size_t)si * N + n) * 3;
   o[0] = (float)u[0];

@@ -43,6 +43,7 @@ struct DevPlan {
   const int* local_slot;       // [Lt]
   const float* local_x0;       // [3][Lt] reference coordinates relative to the chunk origin
   const int* slot_row;         // [N+1]
+  const int2* local_srow;      // [Lt] slot range of each local node's node
   int E, N, Lt;
 };
 
@@ -599,14 +600,13 @@ __device__ __forceinline__ void store_node(const FusedArgs& A, double* const (&u
 }
 
 // S^n of node g from S^{n-1} (prv buffer) and the halo of step n-1: the sum of its
-// slots in fixed order, then the update.  Every chunk touching g computes the same bits.
+// slots [s0, s1) in fixed order, then the update.  Every chunk touching g computes the same bits.
 __device__ __forceinline__ void complete_node(const FusedArgs& A, const NodeParams& np, int g,
-                                              double (&u)[3], double (&v)[3], float (&a)[3],
-                                              bool& hit, float (&uf)[3], float (&vf)[3]) {
-  const DevPlan& P = A.P;
+                                              int s0, int s1, double (&u)[3], double (&v)[3],
+                                              float (&a)[3], bool& hit, float (&uf)[3],
+                                              float (&vf)[3]) {
   float fx = 0.f, fy = 0.f, fz = 0.f;
-  const int s1 = P.slot_row[g + 1];
-  for (int s = P.slot_row[g]; s < s1; s++) {
+  for (int s = s0; s < s1; s++) {
     fx = __fadd_rn(fx, A.halo_prv[0][s]);
     fy = __fadd_rn(fy, A.halo_prv[1][s]);
     fz = __fadd_rn(fz, A.halo_prv[2][s]);
@@ -657,10 +657,20 @@ __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams
         vf[k] = (float)A.v_cur[k][g];
       }
     } else {
+      // interior nodes: one slot at a known position; others: their node's slot range
+      int s0, s1;
+      if (l < ch.n_int) {
+        s0 = ch.slot_begin + l;
+        s1 = s0 + 1;
+      } else {
+        const int2 r = P.local_srow[lb];
+        s0 = r.x;
+        s1 = r.y;
+      }
       double u[3], v[3];
       float a[3];
       bool hit;
-      complete_node(A, np, g, u, v, a, hit, uf, vf);
+      complete_node(A, np, g, s0, s1, u, v, a, hit, uf, vf);
       if (own) store_node(A, A.u_cur, A.v_cur, g, u, v, vf, a, hit, false);
     }
     T.p0[l] = make_float4(P.local_x0[lb] + uf[0], P.local_x0[(size_t)P.Lt + lb] + uf[1],
@@ -679,7 +689,7 @@ __device__ __forceinline__ void node_epilogue(const FusedArgs& A, const ChunkInf
 #pragma unroll 4
   for (int l = threadIdx.x; l < L; l += BS) {
     const float4 f = T.acc[l];
-    const int s = P.local_slot[ch.local_begin + l];
+    const int s = l < ch.n_int ? ch.slot_begin + l : P.local_slot[ch.local_begin + l];
     A.halo_cur[0][s] = f.x;
     A.halo_cur[1][s] = f.y;
     A.halo_cur[2][s] = f.z;
@@ -1032,7 +1042,7 @@ static __global__ void __launch_bounds__(256) k_finalize_nodes(FusedArgs A, Node
   double u[3], v[3];
   float a[3], uf[3], vf[3];
   bool hit;
-  complete_node(A, np, g, u, v, a, hit, uf, vf);
+  complete_node(A, np, g, A.P.slot_row[g], A.P.slot_row[g + 1], u, v, a, hit, uf, vf);
   store_node(A, A.u_cur, A.v_cur, g, u, v, vf, a, hit, A.store_acc != 0);
 }
 

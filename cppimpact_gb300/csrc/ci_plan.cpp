@@ -177,9 +177,14 @@ bool build_plan(int N, int E, int npe, const double* xloc, const int* conn, int 
   int lbeg = 0;
   for (int c = 0; c < C; c++) {
     P.chunks[c].local_begin = lbeg;
+    // interior nodes come first in the owned range and have one slot each, so their
+    // slots are contiguous from here
+    P.chunks[c].slot_begin = P.chunks[c].n_own > 0 ? P.slot_row[P.chunks[c].own_begin] : 0;
     for (int gn : chunk_gids[c]) {
       P.local_gid.push_back(gn);
       P.local_slot.push_back(cursor[gn]++);
+      P.local_srow.push_back(P.slot_row[gn]);
+      P.local_srow.push_back(P.slot_row[gn + 1]);
     }
     lbeg += P.chunks[c].n_local;
   }
@@ -270,6 +275,15 @@ bool verify_plan(const Plan& P, const int* conn, std::string* err) {
       }
       if ((l < ch.n_int) != (P.slot_row[gn + 1] - P.slot_row[gn] == 1)) {
         *err = "interior/boundary split does not match the slot counts";
+        return false;
+      }
+      if (l < ch.n_int && (s != ch.slot_begin + l || P.slot_row[gn] != ch.slot_begin + l)) {
+        *err = "interior slots are not contiguous from the chunk's slot_begin";
+        return false;
+      }
+      if (P.local_srow[2 * (size_t)(ch.local_begin + l)] != P.slot_row[gn] ||
+          P.local_srow[2 * (size_t)(ch.local_begin + l) + 1] != P.slot_row[gn + 1]) {
+        *err = "local slot range does not match the node's slot row";
         return false;
       }
       if (s < P.slot_row[gn] || s >= P.slot_row[gn + 1]) {

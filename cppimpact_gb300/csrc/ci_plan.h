@@ -33,6 +33,7 @@ struct ChunkInfo {
   int local_begin;  // offset of this chunk's entries in the local tables
   int n_int;        // interior nodes (touched by this chunk only) are local ids [0, n_int)
   int inst;         // instance of a batched solve (0 for a single mesh)
+  int slot_begin;   // slot of interior node l is slot_begin + l (one slot each)
 };
 
 struct Plan {
@@ -49,6 +50,7 @@ struct Plan {
   std::vector<int> local_gid;        // [sum n_local] plan node id of each local node
   std::vector<int> local_slot;       // [sum n_local] slot of each (chunk, local node)
   std::vector<int> slot_row;         // [N+1] slots of node n: [slot_row[n], slot_row[n+1])
+  std::vector<int> local_srow;       // [2 sum n_local] slot range of each local node's node
 };
 
 // Builds the plan.  chunk_elements / chunk_nodes <= 0 select defaults from the mesh

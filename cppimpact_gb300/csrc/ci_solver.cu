@@ -91,7 +91,7 @@ struct ci_solver {
   DBuf<ci::ChunkInfo> d_chunks;
   DBuf<uint16_t> d_conn;
   DBuf<uint8_t> d_color;
-  DBuf<int> d_lgid, d_lslot, d_slot_row;
+  DBuf<int> d_lgid, d_lslot, d_slot_row, d_lsrow;
   DBuf<float> d_lx0;  // [3][Lt]
   // state (A buffer = d_u/d_v always holds the state between calls; B is the fused
   // path's second buffer)
@@ -126,6 +126,7 @@ struct ci_solver {
     P.color = d_color.p;
     P.local_gid = d_lgid.p;
     P.local_slot = d_lslot.p;
+    P.local_srow = reinterpret_cast<const int2*>(d_lsrow.p);
     P.local_x0 = d_lx0.p;
     P.slot_row = d_slot_row.p;
     P.E = E;
@@ -606,6 +607,7 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   if ((rc = upload(s->d_color, P.color, s->stream))) return rc;
   if ((rc = upload(s->d_lgid, P.local_gid, s->stream))) return rc;
   if ((rc = upload(s->d_lslot, P.local_slot, s->stream))) return rc;
+  if ((rc = upload(s->d_lsrow, P.local_srow, s->stream))) return rc;
   if ((rc = upload(s->d_slot_row, P.slot_row, s->stream))) return rc;
   const size_t N = s->N, E = s->E;
   CI_CUDA(s->d_lx0.alloc(3 * (size_t)s->Lt));
