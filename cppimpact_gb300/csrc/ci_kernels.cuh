@@ -204,6 +204,7 @@ __device__ __forceinline__ void element_force(const ElemParams& p, const DevStat
   using R = Rule<NPE>;
 #pragma unroll
   for (int i = 0; i < NPE; i++) f[i][0] = f[i][1] = f[i][2] = 0.f;
+  float ve = 0.f;  // this element's volume (vol accumulates over the thread's elements)
 #pragma unroll
   for (int q = 0; q < R::NQ; q++) {
     float G[NPE][3];
@@ -222,6 +223,7 @@ __device__ __forceinline__ void element_force(const ElemParams& p, const DevStat
     if (!(detJ > 0.f)) atomicOr(S.status, (unsigned)ST_DEGENERATE);
     const float wd = R::W * detJ;
     vol += wd;
+    ve += wd;
     if (MODE == EM_MASS_ROWSUM || MODE == EM_MASS_HRZ) {
       float N[NPE];
       R::shape(q, N);
@@ -305,7 +307,7 @@ __device__ __forceinline__ void element_force(const ElemParams& p, const DevStat
   }
   if (MODE == EM_MASS_HRZ && NPE == 10) {
     // HRZ for the straight-sided tet10: rho V/36 at corners, 4 rho V/27 at edges.
-    const float mv = p.rho * vol;
+    const float mv = p.rho * ve;
 #pragma unroll
     for (int i = 0; i < NPE; i++) f[i][0] = i < 4 ? mv * (1.f / 36.f) : mv * (4.f / 27.f);
   }

@@ -28,12 +28,15 @@ def solver(cilib, m, mode, lumping=None, **kw):
                         lumping=lumping, **kw)
 
 
-@pytest.mark.parametrize("order,n", [(1, 4), (2, 3)])
+@pytest.mark.parametrize("order,n", [(1, 4), (2, 3), (1, 10), (2, 8)])
 @pytest.mark.parametrize("lump", ["rowsum", "hrz"])
-def test_lumped_mass(cilib, oracle, order, n, lump):
+@pytest.mark.parametrize("chunks", [(0, 0), (4096, 896)], ids=["auto", "big"])
+def test_lumped_mass(cilib, oracle, order, n, lump, chunks):
+    """Big chunks give the mass kernel several elements per thread (a per-thread volume
+    sum must not leak into the next element's HRZ masses)."""
     m = mg.cube(n, order)
     lp = cilib.LUMP_HRZ if lump == "hrz" else cilib.LUMP_ROWSUM
-    s = solver(cilib, m, cilib.MODE_J2, lumping=lp)
+    s = solver(cilib, m, cilib.MODE_J2, lumping=lp, chunk_elements=chunks[0], chunk_nodes=chunks[1])
     got = s.lumped_mass()
     ref = oracle.lumped_mass(m.xloc, m.conn, oracle.params(E, NU, RHO, lumping=lp))
     assert rel(got, ref) < 1e-6
@@ -158,11 +161,15 @@ def test_refcompat_trajectory_vs_reference_tet4(cilib):
     assert rel(st["x"] - g["xloc"], g["x"] - g["xloc"]) < 1e-3
 
 
-@pytest.mark.parametrize("order,n,steps,speed", [(1, 6, 800, 30.0), (2, 3, 600, 20.0)])
-def test_j2_trajectory_vs_fp64(cilib, oracle, order, n, steps, speed):
+@pytest.mark.parametrize("order,n,steps,speed,chunks", [(1, 6, 800, 30.0, (0, 0)),
+                                                      (2, 3, 600, 20.0, (0, 0)),
+                                                      (2, 4, 600, 20.0, (4096, 896)),
+                                                      (1, 8, 600, 30.0, (4096, 896))])
+def test_j2_trajectory_vs_fp64(cilib, oracle, order, n, steps, speed, chunks):
     m = mg.cube(n, order)
     setup = mg.impact_setup(m, speed, 1e-4)
-    s = _run_gpu(cilib, m, setup, cilib.MODE_J2, steps)
+    s = _run_gpu(cilib, m, setup, cilib.MODE_J2, steps, chunk_elements=chunks[0],
+                 chunk_nodes=chunks[1])
     st = s.state()
     ref = _run_oracle(oracle, m, setup, oracle.J2, steps, oracle.LUMP_HRZ)
     assert ref["epbar"].max() > 0, "the case must yield"
@@ -194,6 +201,8 @@ def test_chunking_does_not_change_physics(cilib):
     a = _run_gpu(cilib, m, setup, cilib.MODE_J2, 200).state()
     b = _run_gpu(cilib, m, setup, cilib.MODE_J2, 200, chunk_elements=37, chunk_nodes=200).state()
     assert rel(a["x"] - m.xloc, b["x"] - m.xloc) < 1e-5
+    c = _run_gpu(cilib, m, setup, cilib.MODE_J2, 200, chunk_elements=4096, chunk_nodes=896).state()
+    assert rel(a["x"] - m.xloc, c["x"] - m.xloc) < 1e-5
 
 
 def test_solve_loop_count_matches_reference(cilib):
