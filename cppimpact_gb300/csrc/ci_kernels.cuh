@@ -17,19 +17,10 @@
 #pragma once
 #include <cstdint>
 
-#include "ci_fpconv.h"
 #include "ci_plan.h"
-
-// State conversions of the nodal update: 0 = hardware (FP64 unit), 1 = integer pipe
-// both ways (ci_fpconv.h), 2 = integer pipe for FP32 -> FP64 only.
-#ifndef CI_INT_CVT
-#define CI_INT_CVT 0
-#endif
 
 namespace ci {
 
-__device__ __forceinline__ float st_f32(double x) { return CI_INT_CVT == 1 ? f64_to_f32(x) : (float)x; }
-__device__ __forceinline__ double st_f64(float x) { return CI_INT_CVT >= 1 ? f32_to_f64(x) : (double)x; }
 
 enum ElemMode { EM_J2 = 0, EM_REFCOMPAT = 1, EM_MASS_ROWSUM = 2, EM_MASS_HRZ = 3 };
 
@@ -553,14 +544,14 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     un[k] = __fma_rn(p.dt, v[k], u[k]);
-    uf[k] = st_f32(un[k]);
+    uf[k] = (float)un[k];
   }
   // |d32 - d| <= 2^-22 (|d0| + |u|_1) for |n_k| <= 1; 1e-6 (1 + ...) covers it
   const float d32 = __fadd_rn(d0f, __fadd_rn(__fmul_rn(p.nf[0], uf[0]),
                                   __fadd_rn(__fmul_rn(p.nf[1], uf[1]), __fmul_rn(p.nf[2], uf[2]))));
   const float margin = 1e-6f * (1.f + fabsf(d0f) + fabsf(uf[0]) + fabsf(uf[1]) + fabsf(uf[2]));
   in_contact = false;
-  double ad[3] = {st_f64(a[0]), st_f64(a[1]), st_f64(a[2])};
+  double ad[3] = {(double)a[0], (double)a[1], (double)a[2]};
   if (!(d32 > margin)) {
     const double d = __fma_rn(p.wall_n[2], un[2], __fma_rn(p.wall_n[1], un[1],
                               __fma_rn(p.wall_n[0], un[0], d0[g])));
@@ -570,7 +561,7 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         ad[k] = __fma_rn(c, p.wall_n[k], ad[k]);
-        a[k] = st_f32(ad[k]);
+        a[k] = (float)ad[k];
       }
     }
   }
@@ -579,7 +570,7 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
     v[k] = __fma_rn(p.dt, ad[k], v[k]);
     u[k] = un[k];
     uf_out[k] = uf[k];
-    vf_out[k] = st_f32(v[k]);
+    vf_out[k] = (float)v[k];
   }
 }
 
@@ -1063,7 +1054,7 @@ __global__ void __launch_bounds__(256) k_node_init(NodeArrays A, NodeParams p_ar
   for (int k = 0; k < 3; k++) {
     u[k] = A.u[k][n];
     v[k] = A.v[k][n];
-    uf[k] = st_f32(u[k]);
+    uf[k] = (float)u[k];
     ad[k] = (double)p.gf[k];
   }
   const float d32 = __fadd_rn(d0f[n], __fadd_rn(__fmul_rn(p.nf[0], uf[0]),

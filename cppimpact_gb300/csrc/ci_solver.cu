@@ -118,6 +118,7 @@ struct ci_solver {
 
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
+  cudaGraphExec_t graph_cont = nullptr;  // fused path: a block that continues a chained one
 
   ci::DevPlan dev_plan() const {
     ci::DevPlan P;
@@ -308,14 +309,17 @@ cudaError_t launch_finalize(ci_solver* s, const ci::FusedArgs& F) {
   return cudaGetLastError();
 }
 
-// n fused steps from the state in buffer A, ending with the state in buffer A.
-cudaError_t enqueue_fused(ci_solver* s, int n) {
+// n fused steps.  start_final: the complete state S^0 is in buffer A (else S^{-1} is in
+// buffer B with the halo of the step before; the blocks of even length that chain
+// without completing the nodes leave it so).  finish: complete S^n into buffer A.
+cudaError_t enqueue_fused(ci_solver* s, int n, bool start_final = true, bool finish = true) {
   if (n <= 0) return cudaSuccess;
   cudaError_t e;
   for (int i = 0; i < n; i++) {
-    const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0, false);
+    const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0 && start_final, false);
     if ((e = launch_fused(s, F))) return e;
   }
+  if (!finish) return cudaSuccess;
   // S^n from S^{n-1} (prv) and the halo of step n-1 (with the accelerations a^n)
   const ci::FusedArgs F = s->fused_args((n & 1) == 0, n & 1, false, true);
   if ((e = launch_finalize(s, F))) return e;
@@ -450,27 +454,42 @@ int compute_mass(ci_solver* s) {
 
 void destroy_graph(ci_solver* s) {
   if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->graph_cont) cudaGraphExecDestroy(s->graph_cont);
   s->graph = nullptr;
+  s->graph_cont = nullptr;
   s->graph_steps = 0;
 }
 
 bool fused_path(const ci_solver* s) { return s->opt.step_kernel == 0; }
 
-int build_graph(ci_solver* s, int steps) {
-  destroy_graph(s);
+int capture(ci_solver* s, cudaGraphExec_t* out, int steps, bool first) {
   cudaGraph_t g = nullptr;
   CI_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
   if (fused_path(s))
-    err = enqueue_fused(s, steps);
+    err = enqueue_fused(s, steps, first, false);
   else
     for (int i = 0; i < steps && err == cudaSuccess; i++) err = enqueue_step(s, false);
   cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
   if (err != cudaSuccess) return fail(CI_ERR_CUDA, "graph capture: %s", cudaGetErrorString(err));
   if (e2 != cudaSuccess) return fail(CI_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e2));
-  err = cudaGraphInstantiate(&s->graph, g, 0);
+  err = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
   if (err != cudaSuccess) return fail(CI_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(err));
+  return CI_OK;
+}
+
+// Fused path: `graph` runs G steps from a complete state, `graph_cont` G steps that
+// continue a previous block; neither completes the nodes at its end, so blocks chain
+// and one k_finalize_nodes closes the call.  Two-kernel path: `graph` only.
+int build_graph(ci_solver* s, int steps) {
+  destroy_graph(s);
+  int rc = capture(s, &s->graph, steps, true);
+  if (!rc && fused_path(s)) rc = capture(s, &s->graph_cont, steps, false);
+  if (rc) {
+    destroy_graph(s);
+    return rc;
+  }
   s->graph_steps = steps;
   return CI_OK;
 }
@@ -479,20 +498,22 @@ int build_graph(ci_solver* s, int steps) {
 int enqueue_steps(ci_solver* s, int n) {
   if (n <= 0) return CI_OK;
   if (fused_path(s)) {
-    // graphs of G (even) steps + boundary finalize, then the remainder directly
+    // chained graphs of G (even) steps, then the remainder directly and the completion
     const int G = (s->opt.graph_steps > 0 ? s->opt.graph_steps : 32) & ~1;
     int rest = n;
+    bool chained = false;
     if (G >= 2 && rest > G) {
-      if (!s->graph || s->graph_steps != G) {
+      if (!s->graph || !s->graph_cont || s->graph_steps != G) {
         const int rc = build_graph(s, G);
         if (rc) return rc;
       }
       while (rest > G) {
-        CI_CUDA(cudaGraphLaunch(s->graph, s->stream));
+        CI_CUDA(cudaGraphLaunch(chained ? s->graph_cont : s->graph, s->stream));
+        chained = true;
         rest -= G;
       }
     }
-    CI_CUDA(enqueue_fused(s, rest));
+    CI_CUDA(enqueue_fused(s, rest, !chained, true));
     s->steps_done += n;
     return CI_OK;
   }
