@@ -18,11 +18,19 @@
 //     an error flag, frees its TMEM and returns) before the stage is overwritten.
 // The epilogue reads the accumulator with tcgen05.ld (each warp its 32 TMEM lanes =
 // 32 rows), applies alpha, beta, bias, tanh and stores.
+//
+// C = A B^T with both operands K-major (transA = 0, transB = 1), M >= 128 and aligned
+// rows takes a pipelined kernel instead: TMA (cp.async.bulk.tensor, 128-byte swizzle)
+// streams 128 x 64 and BN x 64 tiles through a 4-stage shared-memory ring, one thread
+// issues the TMA loads, one thread the MMAs, and mbarriers hand stages back and forth
+// (full: TMA bytes landed; empty: the MMAs reading a stage completed).
+#include <cuda.h>  // CUtensorMap and its enums; the encoder is fetched at run time
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include "../../include/cppimpact_gb300.h"
@@ -205,6 +213,167 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16* __restri
                  : "memory");
 }
 
+constexpr int TBK = 64;      // K per stage: 64 BF16 = one 128-byte swizzle row
+constexpr int TSTAGES = 4;
+
+// Shared-memory descriptor of a K-major tile in the 128-byte swizzled layout TMA writes
+// (rows of 128 bytes, 8-row groups 1024 bytes apart); LBO is unused for this layout.
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;            // LBO (ignored) = 16 B
+  d |= (uint64_t)(1024 >> 4) << 32;  // SBO: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;            // descriptor version
+  d |= (uint64_t)2 << 61;            // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+      "%3}], [%4];\n" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+template <int BN>
+__global__ void __launch_bounds__(128, 1)
+    k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+               float* C, int ldc, __nv_bfloat16* Cb, int M, int N, int K, float alpha, float beta,
+               const float* __restrict__ bias, int act, int* err, int k_chunk, float* partial) {
+  constexpr int A_BYTES = BM * TBK * 2;
+  constexpr int B_BYTES = BN * TBK * 2;
+  extern __shared__ uint8_t smem_raw[];
+  // the swizzled tiles want 1024-byte alignment (the launch reserves the slack)
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + TSTAGES * A_BYTES;
+  __shared__ __align__(8) uint64_t full[TSTAGES], empty[TSTAGES], done;
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int kb = blockIdx.z * k_chunk;
+  const int ke = min(K, kb + k_chunk);
+  const int ktiles = (ke - kb + TBK - 1) / TBK;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < TSTAGES; s++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&full[s])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&empty[s])) : "memory");
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&done)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  bool ok = true;
+  int issued = 0;
+  if (warp == 0 && lane == 0) {
+    // producer: stage kt waits until the MMAs of stage kt - TSTAGES released its slot
+    for (int kt = 0; kt < ktiles; kt++) {
+      const int s = kt % TSTAGES;
+      if (kt >= TSTAGES && !mbar_wait(smem_u32(&empty[s]), ((kt / TSTAGES) - 1) & 1)) {
+        ok = false;
+        break;
+      }
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
+                       smem_u32(&full[s])),
+                   "r"(A_BYTES + B_BYTES)
+                   : "memory");
+      tma_load_2d(smem_u32(sA + s * A_BYTES), &tmA, kb + kt * TBK, m0, smem_u32(&full[s]));
+      tma_load_2d(smem_u32(sB + s * B_BYTES), &tmB, kb + kt * TBK, n0, smem_u32(&full[s]));
+      issued = kt + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer: 4 x (K = 16) per stage, accumulate in TMEM, release the stage
+    const uint32_t idesc = instr_desc(BM, BN);
+    for (int kt = 0; kt < ktiles; kt++) {
+      const int s = kt % TSTAGES;
+      if (!mbar_wait(smem_u32(&full[s]), (kt / TSTAGES) & 1)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+      for (int kk = 0; kk < TBK / 16; kk++) {
+        const uint64_t da = desc_sw128(smem_u32(sA + s * A_BYTES) + kk * 32);
+        const uint64_t db = desc_sw128(smem_u32(sB + s * B_BYTES) + kk * 32);
+        const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+              smem_u32(&empty[s]))
+          : "memory");
+    }
+    // arrives once every MMA issued above has completed
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+            smem_u32(&done))
+        : "memory");
+  }
+  const bool got = mbar_wait(smem_u32(&done), 0);
+  ok = __syncthreads_and(ok && got) != 0;
+  if (!ok) {
+    // let the TMA loads still in flight land before the shared memory goes away
+    if (warp == 0 && lane == 0)
+      for (int kt = max(0, issued - TSTAGES); kt < issued; kt++)
+        mbar_wait(smem_u32(&full[kt % TSTAGES]), (kt / TSTAGES) & 1);
+    if (tid == 0) atomicExch(err, 1);
+  } else {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const int row = m0 + warp * 32 + lane;
+    for (int c = 0; c < BN; c += 8) {
+      uint32_t r[8];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (row < M && partial) {
+        float* pr = partial + ((size_t)blockIdx.z * M + row) * N;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+          if (n0 + c + j < N) pr[n0 + c + j] = ktiles > 0 ? __uint_as_float(r[j]) : 0.f;
+      } else if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int col = n0 + c + j;
+          if (col >= N) continue;
+          float v = alpha * (ktiles > 0 ? __uint_as_float(r[j]) : 0.f);
+          if (beta != 0.f) v += beta * C[(size_t)row * ldc + col];
+          if (bias) v += bias[col];
+          if (act == 1) v = tanhf(v);
+          C[(size_t)row * ldc + col] = v;
+          if (Cb) Cb[(size_t)row * ldc + col] = __float2bfloat16(v);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN)
+                 : "memory");
+}
+
 // C = alpha sum_z partial[z] (z in order) + beta C + bias, then tanh; BF16 copy.
 __global__ void k_splitk_reduce(const float* partial, int splits, float* C, int ldc,
                                 __nv_bfloat16* Cb, int M, int N, float alpha, float beta,
@@ -226,6 +395,63 @@ __global__ void k_splitk_reduce(const float* partial, int splits, float* C, int 
 float* g_ws[64] = {};
 size_t g_ws_size[64] = {};
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn tensor_map_encoder() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// 2-D map of a row-major BF16 matrix [rows x K] (leading dimension ld), boxes of
+// box_rows x 64 with the 128-byte swizzle; out-of-range elements read as zero.
+bool make_tile_map(CUtensorMap* map, const void* base, int rows, int K, int ld, int box_rows) {
+  const EncodeTiledFn enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)TBK, (cuuint32_t)box_rows};
+  const cuuint32_t es[2] = {1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+             es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN>
+constexpr int tma_smem_bytes() {
+  return TSTAGES * (BM * TBK * 2 + BN * TBK * 2) + 1024;
+}
+
+template <int BN>
+cudaError_t launch_tma(const CUtensorMap& ta, const CUtensorMap& tb, dim3 grid, cudaStream_t st,
+                       float* C, int ldc, __nv_bfloat16* Cb, int M, int N, int K, float alpha,
+                       float beta, const float* bias, int act, int* err, int k_chunk,
+                       float* partial) {
+  static bool configured[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !configured[dev]) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        k_gemm_tma<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, tma_smem_bytes<BN>());
+    if (e != cudaSuccess) return e;
+    configured[dev] = true;
+  }
+  k_gemm_tma<BN><<<grid, 128, tma_smem_bytes<BN>(), st>>>(ta, tb, C, ldc, Cb, M, N, K, alpha, beta,
+                                                         bias, act, err, k_chunk, partial);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 extern "C" int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, int ldb, int transB,
@@ -237,7 +463,14 @@ extern "C" int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, i
   if (activation != 0 && activation != 1)
     return ci::set_last_error(CI_ERR_INVALID, "ci_gemm_bf16: activation must be 0 or 1");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const int bn = N <= 64 ? 64 : 128;
+  // A B^T with both operands K-major and TMA-compatible rows: the pipelined kernel
+  bool tma = !transA && transB && M >= BM && N >= 16 && K >= TBK && lda >= K && ldb >= K &&
+             lda % 8 == 0 && ldb % 8 == 0 && reinterpret_cast<uintptr_t>(A) % 16 == 0 &&
+             reinterpret_cast<uintptr_t>(B) % 16 == 0;
+  const int bn_tma = N <= 64 ? 64 : N <= 128 ? 128 : 256;
+  CUtensorMap ta, tb;
+  tma = tma && make_tile_map(&ta, A, M, K, lda, BM) && make_tile_map(&tb, B, N, K, ldb, bn_tma);
+  const int bn = tma ? bn_tma : (N <= 64 ? 64 : 128);
   const int tiles = ((M + BM - 1) / BM) * ((N + bn - 1) / bn);
   // split K when the output has too few tiles to fill the GPU and K is long
   int splits = 1;
@@ -263,21 +496,32 @@ extern "C" int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, i
     partial = g_ws[dev];
   }
   dim3 grid((M + BM - 1) / BM, (N + bn - 1) / bn, splits);
-  if (bn == 64)
+  __nv_bfloat16* cb = static_cast<__nv_bfloat16*>(C_bf16);
+  cudaError_t le = cudaSuccess;
+  if (tma) {
+    if (bn == 64)
+      le = launch_tma<64>(ta, tb, grid, st, C, ldc, cb, M, N, K, alpha, beta, bias, activation,
+                          d_error, k_chunk, partial);
+    else if (bn == 128)
+      le = launch_tma<128>(ta, tb, grid, st, C, ldc, cb, M, N, K, alpha, beta, bias, activation,
+                           d_error, k_chunk, partial);
+    else
+      le = launch_tma<256>(ta, tb, grid, st, C, ldc, cb, M, N, K, alpha, beta, bias, activation,
+                           d_error, k_chunk, partial);
+    if (le != cudaSuccess) return ci::set_last_error(CI_ERR_CUDA, cudaGetErrorString(le));
+  } else if (bn == 64) {
     k_gemm_bf16<64><<<grid, 128, 0, st>>>(
         static_cast<const __nv_bfloat16*>(A), lda, transA, static_cast<const __nv_bfloat16*>(B),
-        ldb, transB, C, ldc, static_cast<__nv_bfloat16*>(C_bf16), M, N, K, alpha, beta, bias,
-        activation, d_error, k_chunk, partial);
-  else
+        ldb, transB, C, ldc, cb, M, N, K, alpha, beta, bias, activation, d_error, k_chunk, partial);
+  } else {
     k_gemm_bf16<128><<<grid, 128, 0, st>>>(
         static_cast<const __nv_bfloat16*>(A), lda, transA, static_cast<const __nv_bfloat16*>(B),
-        ldb, transB, C, ldc, static_cast<__nv_bfloat16*>(C_bf16), M, N, K, alpha, beta, bias,
-        activation, d_error, k_chunk, partial);
+        ldb, transB, C, ldc, cb, M, N, K, alpha, beta, bias, activation, d_error, k_chunk, partial);
+  }
   if (splits > 1) {
     const long long mn = (long long)M * N;
-    k_splitk_reduce<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(
-        partial, splits, C, ldc, static_cast<__nv_bfloat16*>(C_bf16), M, N, alpha, beta, bias,
-        activation);
+    k_splitk_reduce<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(partial, splits, C, ldc, cb, M, N,
+                                                                  alpha, beta, bias, activation);
   }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return ci::set_last_error(CI_ERR_CUDA, cudaGetErrorString(e));

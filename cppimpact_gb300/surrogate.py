@@ -176,9 +176,11 @@ def pod(S, rank: int, oversample: int = 32, seed: int = 0):
     g = torch.Generator(device="cuda").manual_seed(seed)
     k = rank + oversample
     dofs = S.shape[1]
-    Om = torch.randn((dofs, k), generator=g, device="cuda").to(torch.bfloat16)
+    # the two products with the long dimensions run as A B^T with K-major operands
+    # (the pipelined tensor-core path): Omega is drawn transposed, S^T formed once
+    OmT = torch.randn((k, dofs), generator=g, device="cuda").to(torch.bfloat16)
     Yb = torch.empty((S.shape[0], k), dtype=torch.bfloat16, device="cuda")
-    gemm(S, Om, out_bf16=Yb)                               # Y = S Omega
+    gemm(S, OmT, transB=True, out_bf16=Yb)                 # Y = S Omega
     G = gemm(Yb, Yb, transA=True).double().cpu().numpy()   # Y^T Y
     w, U = jacobi_eigh(G)
     keep = w > w[0] * 1e-10
@@ -186,7 +188,9 @@ def pod(S, rank: int, oversample: int = 32, seed: int = 0):
     Rb = torch.tensor(Rinv, dtype=torch.float32, device="cuda").to(torch.bfloat16).contiguous()
     Qb = torch.empty((S.shape[0], Rb.shape[1]), dtype=torch.bfloat16, device="cuda")
     gemm(Yb, Rb, out_bf16=Qb)
-    W = gemm(S, Qb, transA=True).double().cpu().numpy()    # W = S^T Q  [dofs x k]
+    St = S.t().contiguous()
+    W = gemm(St, Qb.t().contiguous(), transB=True).double().cpu().numpy()  # W = S^T Q [dofs x k]
+    del St
     w2, U2 = jacobi_eigh(W.T @ W)
     V = W @ U2[:, :rank] / np.sqrt(np.maximum(w2[:rank], 1e-300))[None, :]
     # orthonormalise (modified Gram-Schmidt, FP64)
@@ -269,7 +273,7 @@ class Surrogate:
         Phi, sv = pod(S, cfg.rank, seed=cfg.seed)
         self.Phi = Phi
         self.Phib = torch.tensor(Phi, dtype=torch.float32, device="cuda").to(torch.bfloat16).contiguous()
-        A = gemm(S, self.Phib)                              # modal trajectories [n*k x r]
+        A = gemm(S, self.Phib.t().contiguous(), transB=True)  # modal trajectories [n*k x r]
         torch.cuda.synchronize()
         self.timings["pod_s"] = time.perf_counter() - t0
         rel = float((S.float() - gemm(A.to(torch.bfloat16).contiguous(), self.Phib, transB=True)).norm()
@@ -398,16 +402,17 @@ def _errstats(e: np.ndarray) -> dict:
 
 
 def gemm_tflops(rows: int, dofs: int, k: int, reps: int = 5) -> dict:
-    """Throughput of the POD's largest product, W = S^T Q ([dofs x rows] x [rows x k])."""
+    """Throughput of the POD's largest product, W = S^T Q ([dofs x rows] x [rows x k]),
+    run as A B^T with K-major operands."""
     torch = _torch()
-    S = torch.randn((rows, dofs), device="cuda").to(torch.bfloat16)
-    Q = torch.randn((rows, k), device="cuda").to(torch.bfloat16)
+    St = torch.randn((dofs, rows), device="cuda").to(torch.bfloat16)   # S^T, K-major
+    Qt = torch.randn((k, rows), device="cuda").to(torch.bfloat16)      # Q^T, K-major
     out = torch.empty((dofs, k), dtype=torch.float32, device="cuda")
-    gemm(S, Q, transA=True, out=out)
+    gemm(St, Qt, transB=True, out=out)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(reps):
-        gemm(S, Q, transA=True, out=out)
+        gemm(St, Qt, transB=True, out=out)
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps

@@ -222,7 +222,9 @@ int ci_batch_node_order(ci_batch* b, int i, int* perm, int* node_offset);
  * 128-row tiles and K is long, K is split across CTAs: partial tiles go to a per-device
  * FP32 workspace (grown by cudaMalloc on first need) and are summed in a fixed order, so
  * results are deterministic; concurrent calls on different streams of one device must
- * not overlap. */
+ * not overlap.  C = A B^T with both operands K-major (transA = 0, transB = 1), M >= 128,
+ * K >= 64, 16-byte aligned A and B and leading dimensions that are multiples of 8 runs
+ * on a TMA-fed pipelined kernel; other forms on a kernel that stages operands itself. */
 int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, int ldb, int transB, float* C,
                  int ldc, void* C_bf16, int M, int N, int K, float alpha, float beta,
                  const float* bias, int activation, int* d_error, void* stream);

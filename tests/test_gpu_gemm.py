@@ -78,3 +78,21 @@ def test_gemm_bias_tanh_beta(cilib):
     C0 = rng.standard_normal((300, 256))
     c, ref, _ = _gemm(cilib, torch, A, B, 0, 0, beta=0.5, C0=C0)
     assert np.linalg.norm(c - ref) <= 1e-3 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (256, 128, 512), (200, 100, 136), (1000, 300, 1000),
+                                   (384, 96, 20000), (129, 16, 64), (640, 256, 4096)])
+def test_gemm_bf16_nt_pipelined(cilib, M, N, K):
+    """A B^T with K-major operands: the TMA + tcgen05 pipelined path (ragged tiles are
+    zero-filled by TMA; long K is split with a fixed-order reduction)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(M + 3 * N + 7 * K)
+    A = rng.standard_normal((M, K))
+    B = rng.standard_normal((N, K))
+    bias = rng.standard_normal(N)
+    c, ref, cb = _gemm(cilib, torch, A, B, 0, 1, bias=bias)
+    assert np.linalg.norm(c - ref) <= 1e-3 * np.linalg.norm(ref)
+    c2, _, _ = _gemm(cilib, torch, A, B, 0, 1, bias=bias)
+    assert np.array_equal(c, c2)
+    c3, ref3, _ = _gemm(cilib, torch, A * 0.1, B * 0.1, 0, 1, act=1, beta=0.5, C0=rng.standard_normal((M, N)))
+    assert np.abs(c3 - ref3).max() < 5e-3
