@@ -401,22 +401,36 @@ def _errstats(e: np.ndarray) -> dict:
                 max=float(e.max()), frac_over_2pct=float((e > 0.02).mean()))
 
 
-def gemm_tflops(rows: int, dofs: int, k: int, reps: int = 5) -> dict:
+def _time_gemm(A, B, out, reps):
+    torch = _torch()
+    gemm(A, B, transB=True, out=out)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        gemm(A, B, transB=True, out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def gemm_tflops(rows: int, dofs: int, k: int, reps: int = 5, square: int = 8192) -> dict:
     """Throughput of the POD's largest product, W = S^T Q ([dofs x rows] x [rows x k]),
-    run as A B^T with K-major operands."""
+    run as A B^T with K-major operands (its arithmetic intensity is ~k/2 flop per byte
+    of S, so HBM bounds it), and of a square A B^T of side `square` (tensor bound)."""
     torch = _torch()
     St = torch.randn((dofs, rows), device="cuda").to(torch.bfloat16)   # S^T, K-major
     Qt = torch.randn((k, rows), device="cuda").to(torch.bfloat16)      # Q^T, K-major
     out = torch.empty((dofs, k), dtype=torch.float32, device="cuda")
-    gemm(St, Qt, transB=True, out=out)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(reps):
-        gemm(St, Qt, transB=True, out=out)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    return dict(shape=[dofs, k, rows], ms=ms, tflops=2.0 * rows * dofs * k / (ms * 1e-3) / 1e12)
+    ms = _time_gemm(St, Qt, out, reps)
+    pod = dict(shape=[dofs, k, rows], ms=ms, tflops=2.0 * rows * dofs * k / (ms * 1e-3) / 1e12,
+               hbm_gbs=(St.numel() + Qt.numel()) * 2 / (ms * 1e-3) / 1e9)
+    del St, Qt, out
+    A = torch.randn((square, square), device="cuda").to(torch.bfloat16)
+    B = torch.randn((square, square), device="cuda").to(torch.bfloat16)
+    out = torch.empty((square, square), dtype=torch.float32, device="cuda")
+    ms = _time_gemm(A, B, out, reps)
+    sq = dict(shape=[square] * 3, ms=ms, tflops=2.0 * square ** 3 / (ms * 1e-3) / 1e12)
+    return dict(pod=pod, square=sq)
 
 
 def study(cfg: Config, plain_sample: int = 4, audit_fail_fraction: float = 0.1) -> dict:

@@ -127,4 +127,4 @@ def test_small_study_audit_and_fallback(cilib):
     assert r["errors"]["final_peak_disp"]["max"] <= r["errors"]["surrogate_only_peak_disp"]["max"] + 1e-12
     rph = r["runs_per_hour"]
     assert rph["surrogate"] > 0 and rph["plain_gpu_solver"] > 0 and rph["batched_solver"] > 0
-    assert r["gemm"]["tflops"] > 0
+    assert r["gemm"]["pod"]["tflops"] > 0 and r["gemm"]["square"]["tflops"] > 0
