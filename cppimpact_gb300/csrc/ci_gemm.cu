@@ -348,22 +348,43 @@ __global__ void __launch_bounds__(128, 1)
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
       if (row < M && partial) {
-        float* pr = partial + ((size_t)blockIdx.z * M + row) * N;
+        float* pr = partial + ((size_t)blockIdx.z * M + row) * N + n0 + c;
+        if (n0 + c + 8 <= N && (reinterpret_cast<uintptr_t>(pr) & 15) == 0 && ktiles > 0) {
+          reinterpret_cast<float4*>(pr)[0] = make_float4(__uint_as_float(r[0]), __uint_as_float(r[1]),
+                                                         __uint_as_float(r[2]), __uint_as_float(r[3]));
+          reinterpret_cast<float4*>(pr)[1] = make_float4(__uint_as_float(r[4]), __uint_as_float(r[5]),
+                                                         __uint_as_float(r[6]), __uint_as_float(r[7]));
+        } else {
 #pragma unroll
-        for (int j = 0; j < 8; j++)
-          if (n0 + c + j < N) pr[n0 + c + j] = ktiles > 0 ? __uint_as_float(r[j]) : 0.f;
+          for (int j = 0; j < 8; j++)
+            if (n0 + c + j < N) pr[j] = ktiles > 0 ? __uint_as_float(r[j]) : 0.f;
+        }
       } else if (row < M) {
+        float v[8];
 #pragma unroll
         for (int j = 0; j < 8; j++) {
           const int col = n0 + c + j;
-          if (col >= N) continue;
-          float v = alpha * (ktiles > 0 ? __uint_as_float(r[j]) : 0.f);
-          if (beta != 0.f) v += beta * C[(size_t)row * ldc + col];
-          if (bias) v += bias[col];
-          if (act == 1) v = tanhf(v);
-          C[(size_t)row * ldc + col] = v;
-          if (Cb) Cb[(size_t)row * ldc + col] = __float2bfloat16(v);
+          v[j] = alpha * (ktiles > 0 ? __uint_as_float(r[j]) : 0.f);
+          if (col < N) {
+            if (beta != 0.f) v[j] += beta * C[(size_t)row * ldc + col];
+            if (bias) v[j] += bias[col];
+            if (act == 1) v[j] = tanhf(v[j]);
+          }
         }
+        float* crow = C + (size_t)row * ldc + n0 + c;
+        if (n0 + c + 8 <= N && (reinterpret_cast<uintptr_t>(crow) & 15) == 0) {
+          // this thread's 8 columns of its row as two 16-byte stores
+          reinterpret_cast<float4*>(crow)[0] = make_float4(v[0], v[1], v[2], v[3]);
+          reinterpret_cast<float4*>(crow)[1] = make_float4(v[4], v[5], v[6], v[7]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 8; j++)
+            if (n0 + c + j < N) crow[j] = v[j];
+        }
+        if (Cb)
+#pragma unroll
+          for (int j = 0; j < 8; j++)
+            if (n0 + c + j < N) Cb[(size_t)row * ldc + n0 + c + j] = __float2bfloat16(v[j]);
       }
     }
   }
