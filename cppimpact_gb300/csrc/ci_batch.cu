@@ -813,11 +813,9 @@ int ci_batch_run_snapshots(ci_batch* b, int every, float* d_snap, int max_snaps,
   // enqueue_run launches ceil((max_steps + 1) / every) graphs of `every` steps
   {
     const int total = G.max_steps + 1;
-    cudaStream_t st = G.stream;
     // same preparation as a normal run, with the snapshot graph
     const int rc = enqueue_run_graph(G, total, every);
     if (rc) return rc;
-    (void)st;
   }
   CB_CUDA(cudaEventRecord(b->ev1, G.stream));
   CB_CUDA(cudaEventSynchronize(b->ev1));
