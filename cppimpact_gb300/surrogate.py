@@ -44,10 +44,10 @@ class Config:
     hidden: int = 256
     n_train: int = 4096
     n_test: int = 512
-    epochs: int = 600
+    epochs: int = 1500
     batch: int = 256
     lr: float = 2e-3
-    ensemble: int = 3
+    ensemble: int = 5
     spread_threshold: float = 0.01
     audit_fraction: float = 0.05
     error_threshold: float = 0.02
