@@ -228,7 +228,7 @@ def run_ours(args, rank, world):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    fused = args.step_kernel != 1  # 0: one fused kernel, 2: node pass + element kernel
+    fused = args.step_kernel == 0
     kbytes = step_bytes if fused else elem_bytes
     achieved = kbytes / (k_elem_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm",

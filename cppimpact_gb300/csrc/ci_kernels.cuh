@@ -35,8 +35,6 @@ struct DevPlan {
   const float* local_x0;       // [3][Lt] reference coordinates relative to the chunk origin
   const int* slot_row;         // [N+1]
   const int2* local_srow;      // [Lt] slot range of each local node's node
-  const int* node_entry_row;   // [N+1] split path: local entries of node n are
-  const int* node_entries;     //   node_entries[node_entry_row[n] .. node_entry_row[n+1])
   int E, N, Lt;
 };
 
@@ -486,9 +484,6 @@ struct FusedArgs {
   float* epbar;
   double* chunk_work;
   unsigned int* status;
-  // split path: the node pass writes every local entry's shared-memory record here
-  float4* staged0;  // [Lt] (x, y, z, du_x)
-  float2* staged1;  // [Lt] (du_y, du_z)
   int state_final;  // every node already holds S^n in the cur buffer (first step of a call)
   int store_acc;
   // batched solves (k_step<..., BATCH = true>): per-instance parameters and step counts;
@@ -678,17 +673,6 @@ __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams
   }
 }
 
-// Split path: the chunk's records, written by k_node_pass, into shared memory.
-template <int BS>
-__device__ __forceinline__ void load_staged(const FusedArgs& A, const ChunkInfo& ch, const Tile& T) {
-#pragma unroll 4
-  for (int l = threadIdx.x; l < ch.n_local; l += BS) {
-    T.p0[l] = A.staged0[ch.local_begin + l];
-    T.p1[l] = A.staged1[ch.local_begin + l];
-    T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-}
-
 // Every local node's partial force of this step to its slot in the halo.
 template <int BS>
 __device__ __forceinline__ void node_epilogue(const FusedArgs& A, const ChunkInfo& ch,
@@ -717,7 +701,7 @@ __device__ __forceinline__ void add_chunk_work(const FusedArgs& A, float wint, f
 }
 
 // Fused step, one thread per element (tet4, and the tet10 reference variant).
-template <int NPE, int MODE, int BS, bool BATCH = false, bool STAGED = false>
+template <int NPE, int MODE, int BS, bool BATCH = false>
 __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
   extern __shared__ float sm[];
   const DevPlan& P = A.P;
@@ -730,10 +714,7 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, Nod
   const Tile T = make_tile(sm, L);
   __shared__ float red[BS / 32];
 
-  if (STAGED)
-    load_staged<BS>(A, ch, T);
-  else
-    stage_nodes<BS>(A, ep, np, ch, cs.state_final, T);
+  stage_nodes<BS>(A, ep, np, ch, cs.state_final, T);
   if (cs.mode == 1) return;
   __syncthreads();
 
@@ -898,7 +879,7 @@ __device__ __forceinline__ void tet10_rs_slot(const Tet10QP& t, const float (&Pm
 }
 
 // 6 CTAs of 128 threads per SM (80 registers) fit the 896-node chunk's shared tile
-template <int MODE, int BS, bool BATCH = false, bool STAGED = false>
+template <int MODE, int BS, bool BATCH = false>
 __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
   extern __shared__ float sm[];
   const DevPlan& P = A.P;
@@ -911,10 +892,7 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
   const Tile T = make_tile(sm, L);
   __shared__ float red[BS / 32];
 
-  if (STAGED)
-    load_staged<BS>(A, ch, T);
-  else
-    stage_nodes<BS>(A, ep, np, ch, cs.state_final, T);
+  stage_nodes<BS>(A, ep, np, ch, cs.state_final, T);
   if (cs.mode == 1) return;
   __syncthreads();
 
@@ -1047,38 +1025,6 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
   __syncthreads();
   node_epilogue<BS>(A, ch, T);
   if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
-}
-
-// Split path, first half of a step: one thread per node completes S^n (or reads it on
-// the first step of a call), the owner update done once instead of in every chunk that
-// touches the node, and writes the shared-memory record of each of the node's local
-// entries (the same bits stage_nodes would produce).
-template <bool FINAL>
-__global__ void __launch_bounds__(256) k_node_pass(FusedArgs A, NodeParams np, float dt) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= A.P.N) return;
-  const DevPlan& P = A.P;
-  float uf[3], vf[3];
-  if (FINAL) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      uf[k] = (float)A.u_cur[k][g];
-      vf[k] = (float)A.v_cur[k][g];
-    }
-  } else {
-    double u[3], v[3];
-    float a[3];
-    bool hit;
-    complete_node(A, np, g, P.slot_row[g], P.slot_row[g + 1], u, v, a, hit, uf, vf);
-    store_node(A, A.u_cur, A.v_cur, g, u, v, vf, a, hit, false);
-  }
-  const int e1 = P.node_entry_row[g + 1];
-  for (int e = P.node_entry_row[g]; e < e1; e++) {
-    const int lb = P.node_entries[e];
-    A.staged0[lb] = make_float4(P.local_x0[lb] + uf[0], P.local_x0[(size_t)P.Lt + lb] + uf[1],
-                                P.local_x0[2 * (size_t)P.Lt + lb] + uf[2], dt * vf[0]);
-    A.staged1[lb] = make_float2(dt * vf[1], dt * vf[2]);
-  }
 }
 
 // S^N of every node after the last fused step of a call: reads S^{N-1} from the prv

@@ -92,9 +92,6 @@ struct ci_solver {
   DBuf<uint16_t> d_conn;
   DBuf<uint8_t> d_color;
   DBuf<int> d_lgid, d_lslot, d_slot_row, d_lsrow;
-  DBuf<int> d_ner, d_nen;       // split path: local entries of each node (CSR)
-  DBuf<float4> d_staged0;       // split path: shared-memory records of every local entry
-  DBuf<float2> d_staged1;
   DBuf<float> d_lx0;  // [3][Lt]
   // state (A buffer = d_u/d_v always holds the state between calls; B is the fused
   // path's second buffer)
@@ -131,8 +128,6 @@ struct ci_solver {
     P.local_gid = d_lgid.p;
     P.local_slot = d_lslot.p;
     P.local_srow = reinterpret_cast<const int2*>(d_lsrow.p);
-    P.node_entry_row = d_ner.p;
-    P.node_entries = d_nen.p;
     P.local_x0 = d_lx0.p;
     P.slot_row = d_slot_row.p;
     P.E = E;
@@ -209,8 +204,6 @@ struct ci_solver {
     F.chunk_work = d_work.p;
     F.status = d_status.p;
     F.state_final = state_final ? 1 : 0;
-    F.staged0 = d_staged0.p;
-    F.staged1 = d_staged1.p;
     F.store_acc = store_acc ? 1 : 0;
     F.inst_ep = nullptr;
     F.inst_np = nullptr;
@@ -247,23 +240,11 @@ cudaError_t configure_step(int bytes) {
   cudaError_t e = cudaFuncSetAttribute(ci::k_step<NPE, ci::EM_J2, BS>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e) return e;
-  if ((e = cudaFuncSetAttribute(ci::k_step<NPE, ci::EM_J2, BS, false, true>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-    return e;
-  if ((e = cudaFuncSetAttribute(ci::k_step<NPE, ci::EM_REFCOMPAT, BS, false, true>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-    return e;
   if (NPE == 10) {
     if ((e = cudaFuncSetAttribute(ci::k_step_qp10<ci::EM_J2, BS>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
       return e;
     if ((e = cudaFuncSetAttribute(ci::k_step_qp10<ci::EM_REFCOMPAT, BS>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-      return e;
-    if ((e = cudaFuncSetAttribute(ci::k_step_qp10<ci::EM_J2, BS, false, true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-      return e;
-    if ((e = cudaFuncSetAttribute(ci::k_step_qp10<ci::EM_REFCOMPAT, BS, false, true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
       return e;
   }
@@ -292,39 +273,21 @@ cudaError_t configure_npe(int bytes) {
                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-template <int NPE, int BS, bool STAGED>
-cudaError_t launch_step_bs(ci_solver* s, const ci::FusedArgs& F, const ci::ElemParams& ep,
-                           const ci::NodeParams& np) {
-  if (NPE == 10 && s->opt.elem_lanes == 4) {
-    if (s->opt.mode != CI_MODE_REFCOMPAT)
-      ci::k_step_qp10<ci::EM_J2, BS, false, STAGED><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
-    else
-      ci::k_step_qp10<ci::EM_REFCOMPAT, BS, false, STAGED><<<s->C, BS, s->smem_bytes, s->stream>>>(
-          F, ep, np);
-    return cudaGetLastError();
-  }
-  if (s->opt.mode != CI_MODE_REFCOMPAT)
-    ci::k_step<NPE, ci::EM_J2, BS, false, STAGED><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
-  else
-    ci::k_step<NPE, ci::EM_REFCOMPAT, BS, false, STAGED><<<s->C, BS, s->smem_bytes, s->stream>>>(
-        F, ep, np);
-  return cudaGetLastError();
-}
-
-// One step of the deferred-completion path: the fused kernel (step_kernel 0), or the
-// node pass followed by the element kernel on the staged records (step_kernel 2).
 template <int NPE, int BS>
 cudaError_t launch_fused_bs(ci_solver* s, const ci::FusedArgs& F, const ci::ElemParams& ep,
                             const ci::NodeParams& np) {
-  if (s->opt.step_kernel != 2) return launch_step_bs<NPE, BS, false>(s, F, ep, np);
-  const unsigned nb = (unsigned)((s->N + 255) / 256);
-  if (F.state_final)
-    ci::k_node_pass<true><<<nb, 256, 0, s->stream>>>(F, np, ep.dt);
+  if (NPE == 10 && s->opt.elem_lanes == 4) {
+    if (s->opt.mode != CI_MODE_REFCOMPAT)
+      ci::k_step_qp10<ci::EM_J2, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
+    else
+      ci::k_step_qp10<ci::EM_REFCOMPAT, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
+    return cudaGetLastError();
+  }
+  if (s->opt.mode != CI_MODE_REFCOMPAT)
+    ci::k_step<NPE, ci::EM_J2, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
   else
-    ci::k_node_pass<false><<<nb, 256, 0, s->stream>>>(F, np, ep.dt);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  return launch_step_bs<NPE, BS, true>(s, F, ep, np);
+    ci::k_step<NPE, ci::EM_REFCOMPAT, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_fused(ci_solver* s, const ci::FusedArgs& F) {
@@ -497,7 +460,7 @@ void destroy_graph(ci_solver* s) {
   s->graph_steps = 0;
 }
 
-bool fused_path(const ci_solver* s) { return s->opt.step_kernel != 1; }
+bool fused_path(const ci_solver* s) { return s->opt.step_kernel == 0; }
 
 int capture(ci_solver* s, cudaGraphExec_t* out, int steps, bool first) {
   cudaGraph_t g = nullptr;
@@ -619,7 +582,7 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
     ci_default_options(&s->opt);
   if (s->opt.mode != CI_MODE_J2 && s->opt.mode != CI_MODE_REFCOMPAT)
     return fail(CI_ERR_INVALID, "unknown mode");
-  if (s->opt.step_kernel < 0 || s->opt.step_kernel > 2)
+  if (s->opt.step_kernel != 0 && s->opt.step_kernel != 1)
     return fail(CI_ERR_INVALID, "unknown step_kernel");
   if (s->opt.block_threads == 0) s->opt.block_threads = 128;
   if (s->opt.elem_lanes == 0) s->opt.elem_lanes = 4;
@@ -672,22 +635,10 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   CI_CUDA(s->d_u.alloc(3 * N));
   CI_CUDA(s->d_v.alloc(3 * N));
   CI_CUDA(s->d_slot.alloc(3 * (size_t)s->S));
-  if (s->opt.step_kernel != 1) {
+  if (s->opt.step_kernel == 0) {
     CI_CUDA(s->d_ub.alloc(3 * N));
     CI_CUDA(s->d_vb.alloc(3 * N));
     CI_CUDA(s->d_halo1.alloc(3 * (size_t)s->S));
-  }
-  if (s->opt.step_kernel == 2) {
-    // node -> local entries (CSR), for the node pass to write each entry's record
-    std::vector<int> row(s->N + 1, 0), ent(P.local_gid.size());
-    for (int g : P.local_gid) row[g + 1]++;
-    for (int n = 0; n < s->N; n++) row[n + 1] += row[n];
-    std::vector<int> cur(row.begin(), row.end() - 1);
-    for (size_t lb = 0; lb < P.local_gid.size(); lb++) ent[cur[P.local_gid[lb]]++] = (int)lb;
-    if ((rc = upload(s->d_ner, row, s->stream))) return rc;
-    if ((rc = upload(s->d_nen, ent, s->stream))) return rc;
-    CI_CUDA(s->d_staged0.alloc(P.local_gid.size()));
-    CI_CUDA(s->d_staged1.alloc(P.local_gid.size()));
   }
   CI_CUDA(s->d_mass.alloc(N));
   CI_CUDA(s->d_d0.alloc(N));

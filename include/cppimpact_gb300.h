@@ -94,8 +94,7 @@ typedef struct ci_options {
   int chunk_elements; /* elements per CTA chunk, 0 = automatic */
   int chunk_nodes;    /* local-node budget per chunk, 0 = automatic */
   int graph_steps;    /* steps captured per CUDA graph, 0 = automatic */
-  int step_kernel;    /* 0 = fused (one launch per step, default), 1 = element + node kernels,
-                         2 = node pass + element kernel on staged records (same bits as 0) */
+  int step_kernel;    /* 0 = fused (one launch per step, default), 1 = element + node kernels */
   int block_threads;  /* threads per chunk CTA of the fused kernel: 64, 128 or 256; 0 = automatic */
   int elem_lanes;     /* tet10 fused kernel: 4 = one lane per Gauss point, 1 = one thread per
                          element; 0 = automatic (4) */

@@ -262,20 +262,3 @@ def test_fused_matches_two_kernel_path(cilib, order):
     assert rel(a["x"] - m.xloc, b["x"] - m.xloc) < 1e-5
     assert rel(a["epbar"], b["epbar"]) < 1e-4
     assert np.array_equal(a["contact"] & 2, b["contact"] & 2)
-
-
-@pytest.mark.parametrize("order,mode", [(1, "j2"), (2, "j2"), (2, "refcompat")])
-def test_split_path_equals_fused(cilib, order, mode):
-    """step_kernel 2 (node pass + element kernel on staged records) computes every node
-    once instead of in each chunk touching it, with the same rounding: bit for bit the
-    fused kernel, across call boundaries too."""
-    m = mg.cube(5, order)
-    setup = mg.impact_setup(m, 20.0, 1e-4)
-    md = cilib.MODE_J2 if mode == "j2" else cilib.MODE_REFCOMPAT
-    a = _run_gpu(cilib, m, setup, md, 77, graph_steps=8)
-    b = _run_gpu(cilib, m, setup, md, 40, graph_steps=8, step_kernel=2)
-    b.step(37)
-    sa, sb = a.state(), b.state()
-    for k in ("x", "v", "sigma", "epbar", "contact"):
-        assert np.array_equal(sa[k], sb[k]), k
-    assert a.energy()["internal"] == b.energy()["internal"]
