@@ -88,6 +88,8 @@ EXPORTS = {
     "ci_steps_done": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "ci_get_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _fp, _fp, _ubp]),
     "ci_set_state": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "ci_save_state": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "ci_load_state": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ci_get_energy": (C.c_int, [C.c_void_p, C.POINTER(CiEnergy)]),
     "ci_get_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint)]),
     "ci_internal_force": (C.c_int, [C.c_void_p, _dp, _dp, _fp, _fp, _dp, _fp, _fp]),
@@ -270,6 +272,14 @@ class Solver:
         x = np.ascontiguousarray(x, dtype=np.float64)
         v = np.ascontiguousarray(v, dtype=np.float64)
         check(lib().ci_set_state(self._h, _d(x), _d(v)))
+
+    def save_state(self, path):
+        """Binary state file for a restart (ci_save_state)."""
+        check(lib().ci_save_state(self._h, os.fsencode(path)))
+
+    def load_state(self, path):
+        """Restore a state file written for the same mesh and options (ci_load_state)."""
+        check(lib().ci_load_state(self._h, os.fsencode(path)))
 
     def energy(self) -> dict:
         e = CiEnergy()

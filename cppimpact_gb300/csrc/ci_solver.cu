@@ -551,6 +551,51 @@ int upload(DBuf<T>& b, const std::vector<T>& h, cudaStream_t st) {
 
 }  // namespace
 
+// ---- binary state file (restart, parity dumps) ----
+// Layout (little-endian, as written by this library): StateHeader, then X [3N] and
+// vel0 [3] (double, caller order), u, v [3][N] (double, plan order), mass [N] (float),
+// contact [N] (u8), sigma_a [E*nq] (float4), sigma_b [E*nq] (float2), epbar [E*nq]
+// (float), chunk work sums [4C] (double).  The plan order is a function of the mesh and
+// the chunk options, which the header records and ci_load_state checks.
+namespace {
+struct StateHeader {
+  char magic[8];
+  int32_t version, N, E, npe, nq, C, mode, lumping, chunk_elements, chunk_nodes, started;
+  int64_t S, Lt, steps_done;
+  double dt;
+};
+const char kStateMagic[8] = {'C', 'I', 'G', 'B', 'S', 'T', 'A', 'T'};
+
+template <typename T>
+int dev_to_file(FILE* f, const T* d, size_t n, cudaStream_t st) {
+  std::vector<T> h(n);
+  if (n) {
+    CI_CUDA(cudaMemcpyAsync(h.data(), d, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+    CI_CUDA(cudaStreamSynchronize(st));
+  }
+  if (n && fwrite(h.data(), sizeof(T), n, f) != n) return fail(CI_ERR_IO, "state file: write failed");
+  return CI_OK;
+}
+
+template <typename T>
+int file_to_dev(FILE* f, T* d, size_t n, cudaStream_t st) {
+  std::vector<T> h(n);
+  if (n && fread(h.data(), sizeof(T), n, f) != n) return fail(CI_ERR_IO, "state file: truncated");
+  if (n) {
+    CI_CUDA(cudaMemcpyAsync(d, h.data(), sizeof(T) * n, cudaMemcpyHostToDevice, st));
+    CI_CUDA(cudaStreamSynchronize(st));
+  }
+  return CI_OK;
+}
+
+struct FileCloser {
+  FILE* f;
+  ~FileCloser() {
+    if (f) fclose(f);
+  }
+};
+}  // namespace
+
 extern "C" {
 
 int ci_abi_version(void) { return CI_ABI_VERSION; }
@@ -811,6 +856,84 @@ int ci_set_state(ci_solver* s, const double* x, const double* v) {
   CI_CUDA(cudaMemcpyAsync(s->d_v.p, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice,
                           s->stream));
   CI_CUDA(cudaStreamSynchronize(s->stream));
+  return CI_OK;
+}
+
+
+int ci_save_state(ci_solver* s, const char* path) {
+  if (!s || !path) return fail(CI_ERR_INVALID, "null argument");
+  int rc = require_started(s);
+  if (rc) return rc;
+  CI_CUDA(cudaSetDevice(s->device));
+  FILE* f = fopen(path, "wb");
+  if (!f) return fail(CI_ERR_IO, "cannot open %s for writing", path);
+  FileCloser fc{f};
+  StateHeader h{};
+  std::memcpy(h.magic, kStateMagic, 8);
+  h.version = 1;
+  h.N = s->N;
+  h.E = s->E;
+  h.npe = s->npe;
+  h.nq = s->nq;
+  h.C = s->C;
+  h.mode = s->opt.mode;
+  h.lumping = s->opt.lumping;
+  h.chunk_elements = s->opt.chunk_elements;
+  h.chunk_nodes = s->opt.chunk_nodes;
+  h.started = 1;
+  h.S = s->S;
+  h.Lt = s->Lt;
+  h.steps_done = s->steps_done;
+  h.dt = s->dt;
+  const size_t N = s->N, Q = (size_t)s->E * s->nq;
+  if (fwrite(&h, sizeof(h), 1, f) != 1 || fwrite(s->X.data(), sizeof(double), 3 * N, f) != 3 * N ||
+      fwrite(s->vel0.data(), sizeof(double), 3, f) != 3)
+    return fail(CI_ERR_IO, "state file: write failed");
+  if ((rc = dev_to_file(f, s->d_u.p, 3 * N, s->stream))) return rc;
+  if ((rc = dev_to_file(f, s->d_v.p, 3 * N, s->stream))) return rc;
+  if ((rc = dev_to_file(f, s->d_mass.p, N, s->stream))) return rc;
+  if ((rc = dev_to_file(f, s->d_contact.p, N, s->stream))) return rc;
+  if ((rc = dev_to_file(f, s->d_sig_a.p, Q, s->stream))) return rc;
+  if ((rc = dev_to_file(f, s->d_sig_b.p, Q, s->stream))) return rc;
+  if ((rc = dev_to_file(f, s->d_epbar.p, Q, s->stream))) return rc;
+  if ((rc = dev_to_file(f, s->d_work.p, 4 * (size_t)s->C, s->stream))) return rc;
+  return CI_OK;
+}
+
+int ci_load_state(ci_solver* s, const char* path) {
+  if (!s || !path) return fail(CI_ERR_INVALID, "null argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  FILE* f = fopen(path, "rb");
+  if (!f) return fail(CI_ERR_IO, "cannot open %s", path);
+  FileCloser fc{f};
+  StateHeader h{};
+  if (fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, kStateMagic, 8) != 0 || h.version != 1)
+    return fail(CI_ERR_IO, "%s is not a state file of this library", path);
+  if (h.N != s->N || h.E != s->E || h.npe != s->npe || h.nq != s->nq || h.C != s->C ||
+      h.S != s->S || h.Lt != s->Lt || h.mode != s->opt.mode || h.lumping != s->opt.lumping ||
+      h.chunk_elements != s->opt.chunk_elements || h.chunk_nodes != s->opt.chunk_nodes)
+    return fail(CI_ERR_INVALID, "state file was written for another mesh, plan or mode");
+  if (!(h.dt > 0.0) || h.steps_done < 0) return fail(CI_ERR_IO, "state file: bad header");
+  const size_t N = s->N, Q = (size_t)s->E * s->nq;
+  std::vector<double> X(3 * N), vel0(3);
+  if (fread(X.data(), sizeof(double), 3 * N, f) != 3 * N || fread(vel0.data(), sizeof(double), 3, f) != 3)
+    return fail(CI_ERR_IO, "state file: truncated");
+  s->X = X;
+  s->vel0 = vel0;
+  int rc = upload_reference(s);
+  if (rc) return rc;
+  destroy_graph(s);
+  if ((rc = file_to_dev(f, s->d_u.p, 3 * N, s->stream))) return rc;
+  if ((rc = file_to_dev(f, s->d_v.p, 3 * N, s->stream))) return rc;
+  if ((rc = file_to_dev(f, s->d_mass.p, N, s->stream))) return rc;
+  if ((rc = file_to_dev(f, s->d_contact.p, N, s->stream))) return rc;
+  if ((rc = file_to_dev(f, s->d_sig_a.p, Q, s->stream))) return rc;
+  if ((rc = file_to_dev(f, s->d_sig_b.p, Q, s->stream))) return rc;
+  if ((rc = file_to_dev(f, s->d_epbar.p, Q, s->stream))) return rc;
+  if ((rc = file_to_dev(f, s->d_work.p, 4 * (size_t)s->C, s->stream))) return rc;
+  s->dt = h.dt;
+  s->steps_done = h.steps_done;
+  s->started = true;
   return CI_OK;
 }
 

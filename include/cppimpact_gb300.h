@@ -153,6 +153,15 @@ int ci_get_state(ci_solver* s, double* x, double* v, double* mass, float* sigma,
                  unsigned char* contact);
 /* Overwrite the nodal state (caller order, [3N] each); used for restarts. */
 int ci_set_state(ci_solver* s, const double* x, const double* v);
+/* Binary state file of a started solver -- the state the reference's export_to_vtk
+ * dumps (include/dynamics.h:113-254) plus everything a restart needs: positions,
+ * velocities, masses, contact history, stored stress and plastic strain at the Gauss
+ * points, energy work sums, dt and the step count.  ci_load_state restores it into a
+ * solver created for the same mesh, mode, lumping and chunk options (checked; otherwise
+ * CI_ERR_INVALID), after which ci_step continues bit for bit as the saved run would
+ * have.  Files are little-endian as written; CI_ERR_IO on open/read/write failures. */
+int ci_save_state(ci_solver* s, const char* path);
+int ci_load_state(ci_solver* s, const char* path);
 int ci_get_energy(ci_solver* s, ci_energy* e);
 /* Device status word: bit0 non-positive det J seen, bit1 non-finite state seen. */
 int ci_get_status(ci_solver* s, unsigned int* status);

@@ -262,3 +262,31 @@ def test_fused_matches_two_kernel_path(cilib, order):
     assert rel(a["x"] - m.xloc, b["x"] - m.xloc) < 1e-5
     assert rel(a["epbar"], b["epbar"]) < 1e-4
     assert np.array_equal(a["contact"] & 2, b["contact"] & 2)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_state_file_restart_is_bitwise(cilib, tmp_path, order):
+    """Save after 90 steps, run 60 more; a fresh solver loading the file and running the
+    same 60 steps ends in the same bits (state, stress, plastic strain, contact,
+    energies).  A file for another mesh is refused."""
+    m = mg.cube(5, order)
+    setup = mg.impact_setup(m, 20.0, 1e-4)
+    a = _run_gpu(cilib, m, setup, cilib.MODE_J2, 90)
+    path = str(tmp_path / "s.bin")
+    a.save_state(path)
+    a.step(60)
+    b = solver(cilib, m, cilib.MODE_J2, wall_normal=setup["wall_normal"],
+               wall_offset=setup["wall_offset"], wall_stiffness=setup["wall_stiffness"])
+    b.load_state(path)
+    b.step(60)
+    sa, sb = a.state(), b.state()
+    for k in ("x", "v", "mass", "sigma", "epbar", "contact"):
+        assert np.array_equal(sa[k], sb[k]), k
+    ea, eb = a.energy(), b.energy()
+    for k in ("kinetic", "internal", "plastic", "contact", "gravity"):
+        assert ea[k] == eb[k], k
+    other = mg.cube(4, order)
+    c = solver(cilib, other, cilib.MODE_J2)
+    with pytest.raises(cilib.CiError) as e:
+        c.load_state(path)
+    assert e.value.code == -1
