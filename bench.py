@@ -287,6 +287,39 @@ def run_ours(args, rank, world):
     return line
 
 
+def cpu_sweep_baseline(inst, nsteps, seconds_budget: float = 6.0, sample: int = 4):
+    """The reference's CPU algorithm (the oracle's restatement: RefCompat elastic law,
+    z-axis wall, so tilt 0) on the sweep's tet4 instances, one thread: a bounded number
+    of steps per instance, extrapolated to its full step count; runs/hour on one core
+    and on all host cores (independent processes)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py as op
+    tet4 = [d for d in inst if d["conn"].shape[1] == 4][:sample]
+    if not tet4:
+        return None
+    run_s = []
+    for d in tet4:
+        # the same cube and speed with the wall untilted (normal +z, 1 mm below)
+        rp = op.ref_params(d["E"], d["nu"], d["rho"], float(d["xloc"][:, 2].min()) - 1e-3,
+                           d["wall_stiffness"], 1)
+        full = nsteps(d)
+        k = 8
+        while True:
+            t0 = time.perf_counter()
+            op.ref_solve(d["xloc"], d["conn"], rp, d["vel"], d["dt"], (k - 1) * d["dt"] + 0.5 * d["dt"],
+                         nthreads=1)
+            t = time.perf_counter() - t0
+            if t > seconds_budget / sample / 4 or k >= full:
+                break
+            k = min(full, k * 4)
+        run_s.append(t * full / k)
+    per_run = float(np.mean(run_s))
+    cores = os.cpu_count() or 1
+    return {"per_core": 3600.0 / per_run, "cores": cores, "all_cores": cores * 3600.0 / per_run,
+            "sample": f"{len(tet4)} tet4 instances, tilt 0, RefCompat law, bounded steps "
+                      f"extrapolated to each instance's full step count, 1 thread"}
+
+
 def run_sweep(args, count=256, sample=16):
     """The batched sweep: runs/hour of the batch (one launch per step per element type)
     and of the plain solver running instances one at a time (device time of a sample,
@@ -326,7 +359,9 @@ def run_sweep(args, count=256, sample=16):
     b.close()
     frac = sum(d["conn"].shape[0] for d in inst[:sample]) / sum(d["conn"].shape[0] for d in inst)
     plain_ms = sum(single_ms) / max(frac, 1e-12)
+    cpu = None if args.no_cpu_baseline else cpu_sweep_baseline(inst, nsteps)
     return {"instances": count, "t_end_s": 2e-3, "batch_device_ms": ms,
+            "cpu_reference_runs_per_hour": cpu,
             "runs_per_hour": count / (ms / 1e3) * 3600.0,
             "plain_gpu_runs_per_hour": count / (plain_ms / 1e3) * 3600.0,
             "speedup_vs_plain_gpu": plain_ms / ms,
