@@ -24,7 +24,7 @@ namespace ci {
 
 enum ElemMode { EM_J2 = 0, EM_REFCOMPAT = 1, EM_MASS_ROWSUM = 2, EM_MASS_HRZ = 3 };
 
-enum StatusBits { ST_DEGENERATE = 1u, ST_NONFINITE = 2u, ST_SYNC_TIMEOUT = 4u };
+enum StatusBits { ST_DEGENERATE = 1u, ST_NONFINITE = 2u };
 
 struct DevPlan {
   const ChunkInfo* chunks;
@@ -701,9 +701,8 @@ __device__ __forceinline__ void add_chunk_work(const FusedArgs& A, float wint, f
 }
 
 // Fused step, one thread per element (tet4, and the tet10 reference variant).
-template <int NPE, int MODE, int BS, bool BATCH>
-__device__ __forceinline__ void step_body(const FusedArgs& A, const ElemParams& ep_arg,
-                                          const NodeParams& np_arg) {
+template <int NPE, int MODE, int BS, bool BATCH = false>
+__global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
   extern __shared__ float sm[];
   const DevPlan& P = A.P;
   const ChunkInfo ch = P.chunks[blockIdx.x];
@@ -768,11 +767,6 @@ __device__ __forceinline__ void step_body(const FusedArgs& A, const ElemParams& 
   __syncthreads();
   node_epilogue<BS>(A, ch, T);
   if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
-}
-
-template <int NPE, int MODE, int BS, bool BATCH = false>
-__global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
-  step_body<NPE, MODE, BS, BATCH>(A, ep_arg, np_arg);
 }
 
 // ---------------------------------------------------------------------------
@@ -885,9 +879,8 @@ __device__ __forceinline__ void tet10_rs_slot(const Tet10QP& t, const float (&Pm
 }
 
 // 6 CTAs of 128 threads per SM (80 registers) fit the 896-node chunk's shared tile
-template <int MODE, int BS, bool BATCH>
-__device__ __forceinline__ void qp10_body(const FusedArgs& A, const ElemParams& ep_arg,
-                                          const NodeParams& np_arg) {
+template <int MODE, int BS, bool BATCH = false>
+__global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
   extern __shared__ float sm[];
   const DevPlan& P = A.P;
   const ChunkInfo ch = P.chunks[blockIdx.x];
@@ -1032,65 +1025,6 @@ __device__ __forceinline__ void qp10_body(const FusedArgs& A, const ElemParams& 
   __syncthreads();
   node_epilogue<BS>(A, ch, T);
   if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
-}
-
-template <int MODE, int BS, bool BATCH = false>
-__global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
-  qp10_body<MODE, BS, BATCH>(A, ep_arg, np_arg);
-}
-
-// ---------------------------------------------------------------------------
-// Persistent multi-step kernels: when every chunk's CTA fits on the GPU at once (a
-// cooperative launch guarantees it), one launch runs nsteps steps, a grid-wide barrier
-// between them replacing the kernel boundary.  The per-step work is the fused kernel's
-// own body, so the results are bit for bit those of one launch per step.  Views: Af for
-// the launch's first step (complete state or a continuation), A0 / A1 for even / odd
-// steps after it.
-// ---------------------------------------------------------------------------
-constexpr unsigned int kGridSpinLimit = 1u << 24;
-
-// Arrive at generation target / gridDim.x of the barrier counter and wait for every CTA
-// (bounded: false on timeout).  Release / acquire at gpu scope order the halo and state
-// writes of one step before the reads of the next.
-__device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int target) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(count, 1u);
-    int good = 0;
-    for (unsigned int it = 0; it < kGridSpinLimit; it++) {
-      unsigned int seen;
-      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(count) : "memory");
-      if (seen >= target) {
-        good = 1;
-        break;
-      }
-      __nanosleep(32);
-    }
-    __threadfence();
-    ok = good;
-  }
-  __syncthreads();
-  return ok != 0;
-}
-
-template <int NPE, int MODE, int BS, bool QP>
-__global__ void __launch_bounds__(BS, QP ? 768 / BS : 0)
-    k_step_persist(const __grid_constant__ FusedArgs Af, const __grid_constant__ FusedArgs A0,
-                   const __grid_constant__ FusedArgs A1, ElemParams ep, NodeParams np, int nsteps,
-                   unsigned int* bar) {
-  for (int i = 0; i < nsteps; i++) {
-    const FusedArgs* A = i == 0 ? &Af : ((i & 1) ? &A1 : &A0);
-    if (QP)
-      qp10_body<MODE, BS, false>(*A, ep, np);
-    else
-      step_body<NPE, MODE, BS, false>(*A, ep, np);
-    if (i + 1 < nsteps && !grid_barrier(bar, (unsigned int)(i + 1) * gridDim.x)) {
-      if (threadIdx.x == 0) atomicOr(A->status, (unsigned)ST_SYNC_TIMEOUT);
-      return;
-    }
-  }
 }
 
 // S^N of every node after the last fused step of a call: reads S^{N-1} from the prv

@@ -119,8 +119,6 @@ struct ci_solver {
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   cudaGraphExec_t graph_cont = nullptr;  // fused path: a block that continues a chained one
-  bool persist = false;                  // all chunks co-resident: multi-step launches
-  DBuf<unsigned int> d_bar;              // grid-barrier counter of the multi-step kernel
 
   ci::DevPlan dev_plan() const {
     ci::DevPlan P;
@@ -311,76 +309,15 @@ cudaError_t launch_finalize(ci_solver* s, const ci::FusedArgs& F) {
   return cudaGetLastError();
 }
 
-// The multi-step kernel this solver's options select (tet10 with 4 lanes: the Gauss-
-// point-parallel body; otherwise one thread per element).
-template <int NPE, int BS>
-const void* persist_kernel(const ci_solver* s) {
-  const bool qp = NPE == 10 && s->opt.elem_lanes == 4;
-  const bool rc = s->opt.mode == CI_MODE_REFCOMPAT;
-  if (qp)
-    return rc ? (const void*)ci::k_step_persist<10, ci::EM_REFCOMPAT, BS, true>
-              : (const void*)ci::k_step_persist<10, ci::EM_J2, BS, true>;
-  return rc ? (const void*)ci::k_step_persist<NPE, ci::EM_REFCOMPAT, BS, false>
-            : (const void*)ci::k_step_persist<NPE, ci::EM_J2, BS, false>;
-}
-
-const void* persist_kernel(const ci_solver* s) {
-  const int bs = s->opt.block_threads;
-  if (s->npe == 4)
-    return bs == 64 ? persist_kernel<4, 64>(s) : bs == 128 ? persist_kernel<4, 128>(s)
-                                                           : persist_kernel<4, 256>(s);
-  return bs == 64 ? persist_kernel<10, 64>(s) : bs == 128 ? persist_kernel<10, 128>(s)
-                                                          : persist_kernel<10, 256>(s);
-}
-
-// Whether every chunk's CTA can be resident at once (then one cooperative launch runs
-// many steps); sets the kernel's shared-memory limit.
-cudaError_t decide_persist(ci_solver* s) {
-  s->persist = false;
-  if (s->opt.step_kernel != 0) return cudaSuccess;
-  int coop = 0, sms = 0, per_sm = 0;
-  cudaError_t e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->device);
-  if (e != cudaSuccess || !coop) return cudaSuccess;
-  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device))) return e;
-  const void* k = persist_kernel(s);
-  if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_bytes)))
-    return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, s->opt.block_threads,
-                                                         s->smem_bytes)))
-    return e;
-  s->persist = (long long)per_sm * sms >= s->C;
-  return cudaSuccess;
-}
-
-// n steps in one cooperative launch of the multi-step kernel (same views and rounding
-// as n launches of the fused kernel).
-cudaError_t launch_persist(ci_solver* s, int n, bool start_final) {
-  const ci::FusedArgs Af = s->fused_args(true, 0, start_final, false);
-  const ci::FusedArgs A0 = s->fused_args(true, 0, false, false);
-  const ci::FusedArgs A1 = s->fused_args(false, 1, false, false);
-  ci::ElemParams ep = s->elem_params((float)s->dt, true);
-  ci::NodeParams np = s->node_params();
-  unsigned int* bar = s->d_bar.p;
-  void* args[] = {(void*)&Af, (void*)&A0, (void*)&A1, (void*)&ep, (void*)&np, (void*)&n, (void*)&bar};
-  cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(unsigned int), s->stream);
-  if (e != cudaSuccess) return e;
-  return cudaLaunchCooperativeKernel(persist_kernel(s), dim3(s->C), dim3(s->opt.block_threads), args,
-                                     s->smem_bytes, s->stream);
-}
-
 // n fused steps.  start_final: the complete state S^0 is in buffer A (else S^{-1} is in
 // buffer B with the halo of the step before; the blocks of even length that chain
 // without completing the nodes leave it so).  finish: complete S^n into buffer A.
 cudaError_t enqueue_fused(ci_solver* s, int n, bool start_final = true, bool finish = true) {
   if (n <= 0) return cudaSuccess;
   cudaError_t e;
-  if (s->persist) {
-    if ((e = launch_persist(s, n, start_final))) return e;
-  } else {
-    for (int i = 0; i < n; i++) {
-      const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0 && start_final, false);
-      if ((e = launch_fused(s, F))) return e;
-    }
+  for (int i = 0; i < n; i++) {
+    const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0 && start_final, false);
+    if ((e = launch_fused(s, F))) return e;
   }
   if (!finish) return cudaSuccess;
   // S^n from S^{n-1} (prv) and the halo of step n-1 (with the accelerations a^n)
@@ -434,7 +371,6 @@ int check_status(ci_solver* s) {
   CI_CUDA(cudaStreamSynchronize(s->stream));
   if (st & ci::ST_DEGENERATE) return fail(CI_ERR_DEGENERATE, "an element has det J <= 0");
   if (st & ci::ST_NONFINITE) return fail(CI_ERR_NONFINITE, "non-finite nodal state");
-  if (st & ci::ST_SYNC_TIMEOUT) return fail(CI_ERR_CUDA, "grid barrier of the multi-step kernel timed out");
   return CI_OK;
 }
 
@@ -524,7 +460,7 @@ void destroy_graph(ci_solver* s) {
   s->graph_steps = 0;
 }
 
-bool fused_path(const ci_solver* s) { return s->opt.step_kernel != 1; }
+bool fused_path(const ci_solver* s) { return s->opt.step_kernel == 0; }
 
 int capture(ci_solver* s, cudaGraphExec_t* out, int steps, bool first) {
   cudaGraph_t g = nullptr;
@@ -566,17 +502,6 @@ int enqueue_steps(ci_solver* s, int n) {
     const int G = (s->opt.graph_steps > 0 ? s->opt.graph_steps : 32) & ~1;
     int rest = n;
     bool chained = false;
-    if (s->persist) {
-      // launches of G (even) steps chained without completing the nodes between them
-      while (G >= 2 && rest > G) {
-        CI_CUDA(enqueue_fused(s, G, !chained, false));
-        chained = true;
-        rest -= G;
-      }
-      CI_CUDA(enqueue_fused(s, rest, !chained, true));
-      s->steps_done += n;
-      return CI_OK;
-    }
     if (G >= 2 && rest > G) {
       if (!s->graph || !s->graph_cont || s->graph_steps != G) {
         const int rc = build_graph(s, G);
@@ -702,7 +627,7 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
     ci_default_options(&s->opt);
   if (s->opt.mode != CI_MODE_J2 && s->opt.mode != CI_MODE_REFCOMPAT)
     return fail(CI_ERR_INVALID, "unknown mode");
-  if (s->opt.step_kernel < 0 || s->opt.step_kernel > 2)
+  if (s->opt.step_kernel != 0 && s->opt.step_kernel != 1)
     return fail(CI_ERR_INVALID, "unknown step_kernel");
   if (s->opt.block_threads == 0) s->opt.block_threads = 128;
   if (s->opt.elem_lanes == 0) s->opt.elem_lanes = 4;
@@ -739,8 +664,6 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   s->vel0.assign(3, 0.0);
 
   CI_CUDA(s->npe == 4 ? configure_npe<4>((int)s->smem_bytes) : configure_npe<10>((int)s->smem_bytes));
-  CI_CUDA(decide_persist(s.get()));
-  if (s->persist) CI_CUDA(s->d_bar.alloc(1));
   CI_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   CI_CUDA(cudaEventCreate(&s->ev0));
   CI_CUDA(cudaEventCreate(&s->ev1));
@@ -757,7 +680,7 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   CI_CUDA(s->d_u.alloc(3 * N));
   CI_CUDA(s->d_v.alloc(3 * N));
   CI_CUDA(s->d_slot.alloc(3 * (size_t)s->S));
-  if (s->opt.step_kernel != 1) {
+  if (s->opt.step_kernel == 0) {
     CI_CUDA(s->d_ub.alloc(3 * N));
     CI_CUDA(s->d_vb.alloc(3 * N));
     CI_CUDA(s->d_halo1.alloc(3 * (size_t)s->S));
@@ -1283,11 +1206,7 @@ int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms) {
   return check_status(s);
 }
 
-int ci_launches_per_step(const ci_solver* s) {
-  if (!s) return -1;
-  if (s->opt.step_kernel == 1) return 2;
-  return s->persist ? 0 : 1;
-}
+int ci_launches_per_step(const ci_solver* s) { return s ? (s->opt.step_kernel == 0 ? 1 : 2) : 0; }
 
 int ci_plan_stats(const ci_mesh* mesh, int chunk_elements, int chunk_nodes, long long* stats,
                   int* perm_elems, int* perm_nodes) {

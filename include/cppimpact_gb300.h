@@ -94,10 +94,7 @@ typedef struct ci_options {
   int chunk_elements; /* elements per CTA chunk, 0 = automatic */
   int chunk_nodes;    /* local-node budget per chunk, 0 = automatic */
   int graph_steps;    /* steps captured per CUDA graph, 0 = automatic */
-  int step_kernel;    /* 0 = fused (default): one cooperative launch per graph_steps steps with
-                         a grid barrier between steps when every chunk fits on the GPU at
-                         once, else one launch per step; 1 = element + node kernels;
-                         2 = fused, always one launch per step (same bits as 0) */
+  int step_kernel;    /* 0 = fused (one launch per step, default), 1 = element + node kernels */
   int block_threads;  /* threads per chunk CTA of the fused kernel: 64, 128 or 256; 0 = automatic */
   int elem_lanes;     /* tet10 fused kernel: 4 = one lane per Gauss point, 1 = one thread per
                          element; 0 = automatic (4) */
@@ -291,9 +288,7 @@ int ci_time_steps(ci_solver* s, int nsteps, float* ms);
  * boundary finalise divided by nsteps; two-kernel path out[0] = element kernel,
  * out[1] = node kernel. */
 int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms);
-/* Kernel launches one step issues in the steady state (for launch accounting): 1 for
- * the fused kernel, 2 for the element + node kernels, 0 when every chunk fits on the GPU
- * at once and one cooperative launch runs up to graph_steps steps. */
+/* Kernel launches one step issues (for launch accounting). */
 int ci_launches_per_step(const ci_solver* s);
 
 /* ---- mesh utilities (host only) ---- */

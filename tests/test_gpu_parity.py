@@ -290,29 +290,3 @@ def test_state_file_restart_is_bitwise(cilib, tmp_path, order):
     with pytest.raises(cilib.CiError) as e:
         c.load_state(path)
     assert e.value.code == -1
-
-
-@pytest.mark.parametrize("order,lanes,mode", [(1, 4, "j2"), (2, 4, "j2"), (2, 1, "j2"),
-                                              (2, 4, "refcompat")])
-def test_multistep_kernel_equals_per_step_launches(cilib, order, lanes, mode):
-    """A mesh whose chunks all fit on the GPU runs many steps per cooperative launch with
-    a grid barrier between steps; the per-step body is the fused kernel's, so the result
-    is bit for bit that of one launch per step (step_kernel 2), across calls of any
-    length."""
-    m = mg.cube(5, order)
-    setup = mg.impact_setup(m, 20.0, 1e-4)
-    md = cilib.MODE_J2 if mode == "j2" else cilib.MODE_REFCOMPAT
-    # HRZ masses: the reference's row-sum tet10 masses are negative at corners and its
-    # force law then loses stability through contact within these steps
-    lp = cilib.LUMP_HRZ
-    a = _run_gpu(cilib, m, setup, md, 77, lumping=lp, graph_steps=8, elem_lanes=lanes)
-    assert a.launches_per_step() == 0
-    b = _run_gpu(cilib, m, setup, md, 40, lumping=lp, graph_steps=8, elem_lanes=lanes, step_kernel=2)
-    assert b.launches_per_step() == 1
-    b.step(37)
-    sa, sb = a.state(), b.state()
-    for k in ("x", "v", "sigma", "epbar", "contact"):
-        assert np.array_equal(sa[k], sb[k]), k
-    ea, eb = a.energy(), b.energy()
-    for k in ("kinetic", "internal", "plastic", "contact"):
-        assert ea[k] == eb[k], k
