@@ -266,7 +266,7 @@ int build_group(ci_batch* b, Group& G, const ci_instance* in, const ci_options& 
       const size_t j = uniq[i];
       const ci_instance& I = in[G.insts[j]];
       ok[j] = build_plan(I.mesh.num_nodes, I.mesh.num_elements, I.mesh.nodes_per_element,
-                         I.mesh.xloc, I.mesh.element_nodes, G.chunk_elements, G.chunk_nodes, 304,
+                         I.mesh.xloc, I.mesh.element_nodes, G.chunk_elements, G.chunk_nodes, kDefaultTargetCtas,
                          &built[j], &errs[j]);
     }
   };

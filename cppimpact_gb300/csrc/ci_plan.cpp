@@ -80,9 +80,9 @@ bool build_plan(int N, int E, int npe, const double* xloc, const int* conn, int 
   std::stable_sort(sfc.begin(), sfc.end(), [&](int a, int b) { return key[a] < key[b]; });
 
   // -- 2. chunks: contiguous runs along the curve bounded by elements and local nodes
-  if (target_ctas <= 0) target_ctas = 304;
+  if (target_ctas <= 0) target_ctas = kDefaultTargetCtas;
   int emax = chunk_elements > 0 ? chunk_elements
-                                : std::max(32, std::min(4096, (E + target_ctas - 1) / target_ctas));
+                                : std::max(16, std::min(4096, (E + target_ctas - 1) / target_ctas));
   int lmax = chunk_nodes > 0 ? chunk_nodes : 896;
   lmax = std::max(lmax, npe);
   std::vector<int> stamp(N, -1), owner(N, -1), touch(N, 0);

@@ -53,8 +53,12 @@ struct Plan {
   std::vector<int> local_srow;       // [2 sum n_local] slot range of each local node's node
 };
 
+// Automatic chunking aims at this many chunks (CTAs) for small meshes: four per SM of a
+// 152-SM GB300.  A constant, so a mesh's plan does not depend on the device.
+constexpr int kDefaultTargetCtas = 608;
+
 // Builds the plan.  chunk_elements / chunk_nodes <= 0 select defaults from the mesh
-// size and target_ctas (roughly two CTAs per SM).
+// size and target_ctas (<= 0: kDefaultTargetCtas).
 bool build_plan(int N, int E, int npe, const double* xloc, const int* conn, int chunk_elements,
                 int chunk_nodes, int target_ctas, Plan* plan, std::string* err);
 

@@ -643,11 +643,9 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   s->nq = s->npe == 4 ? 1 : 4;
   s->device = s->opt.device;
   CI_CUDA(cudaSetDevice(s->device));
-  int sms = 0;
-  CI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
   std::string err;
   if (!ci::build_plan(s->N, s->E, s->npe, mesh->xloc, mesh->element_nodes, s->opt.chunk_elements,
-                      s->opt.chunk_nodes, 2 * sms, &s->plan, &err))
+                      s->opt.chunk_nodes, ci::kDefaultTargetCtas, &s->plan, &err))
     return fail(CI_ERR_INVALID, "%s", err.c_str());
   const ci::Plan& P = s->plan;
   s->C = P.n_chunks;
@@ -1214,7 +1212,7 @@ int ci_plan_stats(const ci_mesh* mesh, int chunk_elements, int chunk_nodes, long
   ci::Plan P;
   std::string err;
   if (!ci::build_plan(mesh->num_nodes, mesh->num_elements, mesh->nodes_per_element, mesh->xloc,
-                      mesh->element_nodes, chunk_elements, chunk_nodes, 304, &P, &err))
+                      mesh->element_nodes, chunk_elements, chunk_nodes, ci::kDefaultTargetCtas, &P, &err))
     return fail(CI_ERR_INVALID, "%s", err.c_str());
   stats[0] = P.n_chunks;
   stats[1] = P.max_colors;
@@ -1234,7 +1232,7 @@ int ci_plan_verify(const ci_mesh* mesh, int chunk_elements, int chunk_nodes) {
   ci::Plan P;
   std::string err;
   if (!ci::build_plan(mesh->num_nodes, mesh->num_elements, mesh->nodes_per_element, mesh->xloc,
-                      mesh->element_nodes, chunk_elements, chunk_nodes, 304, &P, &err))
+                      mesh->element_nodes, chunk_elements, chunk_nodes, ci::kDefaultTargetCtas, &P, &err))
     return fail(CI_ERR_INVALID, "%s", err.c_str());
   if (!ci::verify_plan(P, mesh->element_nodes, &err)) return fail(CI_ERR_INVALID, "%s", err.c_str());
   return CI_OK;
