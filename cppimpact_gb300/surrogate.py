@@ -48,7 +48,6 @@ class Config:
     batch: int = 256
     lr: float = 2e-3
     ensemble: int = 5
-    ep_epochs: int = 400      # the small peak-plastic-strain networks converge sooner
     spread_threshold: float = 0.01
     audit_fraction: float = 0.05
     error_threshold: float = 0.02
@@ -305,7 +304,7 @@ class Surrogate:
             Tn = ((ep - self.ep_mean) / self.ep_std).contiguous()
             for j in range(cfg.ensemble):
                 net = MLP(4, 64, 1, cfg.seed + 303 * j)
-                self._train(net, X, Tn, cfg.seed + 11 * j, epochs=cfg.ep_epochs)
+                self._train(net, X, Tn, cfg.seed + 11 * j)
                 self.ep_nets.append(net)
         torch.cuda.synchronize()
         self.timings["train_s"] = time.perf_counter() - t0
@@ -315,11 +314,10 @@ class Surrogate:
         torch = _torch()
         return torch.tensor(np.asarray(params, dtype=np.float32)[:, 0], device="cuda")
 
-    def _train(self, net, X, T, seed, epochs=None):
+    def _train(self, net, X, T, seed):
         """Adam in three phases of decreasing step size (lr, lr/5, lr/25)."""
         cfg = self.cfg
-        n = cfg.epochs if epochs is None else epochs
-        parts = [n // 2, n // 4, n - n // 2 - n // 4]
+        parts = [cfg.epochs // 2, cfg.epochs // 4, cfg.epochs - cfg.epochs // 2 - cfg.epochs // 4]
         losses = []
         for i, (ep, lr) in enumerate(zip(parts, (cfg.lr, cfg.lr / 5, cfg.lr / 25))):
             if ep > 0:
