@@ -115,6 +115,11 @@ struct ci_solver {
   DBuf<float2> d_sig_b2;
   DBuf<float> d_epbar2;
   DBuf<double> d_epart;
+  // caller-order exchange of x and v (allocated on first use): reference positions and
+  // the plan index of every caller node, and [3N] AoS staging buffers
+  DBuf<double> d_Xc, d_xc, d_vc;
+  DBuf<int> d_node_new;
+  bool xc_stale = true;  // X changed since d_Xc was uploaded
 
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
@@ -596,6 +601,53 @@ struct FileCloser {
 };
 }  // namespace
 
+namespace {
+// x (caller AoS) = X + u (plan SoA), v likewise; one thread per caller node
+__global__ void k_state_to_caller(const double* u, const double* v, const double* Xc,
+                                  const int* node_new, int N, double* xc, double* vc) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int i = node_new[n];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    if (xc) xc[3 * (size_t)n + k] = Xc[3 * (size_t)n + k] + u[(size_t)k * N + i];
+    if (vc) vc[3 * (size_t)n + k] = v[(size_t)k * N + i];
+  }
+}
+
+__global__ void k_state_from_caller(const double* xc, const double* vc, const double* Xc,
+                                    const int* node_new, int N, double* u, double* v) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int i = node_new[n];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    u[(size_t)k * N + i] = xc[3 * (size_t)n + k] - Xc[3 * (size_t)n + k];
+    v[(size_t)k * N + i] = vc[3 * (size_t)n + k];
+  }
+}
+
+// The caller-order exchange buffers; X is uploaded again after it changes
+// (ci_initialize, ci_load_state).
+int ensure_exchange(ci_solver* s) {
+  const size_t n3 = 3 * (size_t)s->N;
+  if (!s->d_xc.p) {
+    CI_CUDA(s->d_xc.alloc(n3));
+    CI_CUDA(s->d_vc.alloc(n3));
+    CI_CUDA(s->d_Xc.alloc(n3));
+    CI_CUDA(s->d_node_new.alloc(s->N));
+    CI_CUDA(cudaMemcpyAsync(s->d_node_new.p, s->plan.node_new.data(), sizeof(int) * s->N,
+                            cudaMemcpyHostToDevice, s->stream));
+  }
+  if (s->xc_stale) {
+    CI_CUDA(cudaMemcpyAsync(s->d_Xc.p, s->X.data(), sizeof(double) * n3, cudaMemcpyHostToDevice,
+                            s->stream));
+    s->xc_stale = false;
+  }
+  return CI_OK;
+}
+}  // namespace
+
 extern "C" {
 
 int ci_abi_version(void) { return CI_ABI_VERSION; }
@@ -719,6 +771,7 @@ int ci_initialize(ci_solver* s, const double pos[3], const double vel[3]) {
   for (int i = 0; i < s->N; i++)
     for (int k = 0; k < 3; k++) s->X[3 * (size_t)i + k] = s->X0[3 * (size_t)i + k] + pos[k];
   for (int k = 0; k < 3; k++) s->vel0[k] = vel[k];
+  s->xc_stale = true;
   int rc = upload_reference(s);
   if (rc) return rc;
   return reset_state(s);
@@ -775,14 +828,20 @@ int ci_get_state(ci_solver* s, double* x, double* v, double* mass, float* sigma,
   CI_CUDA(cudaSetDevice(s->device));
   const int N = s->N, E = s->E, nq = s->nq;
   const ci::Plan& P = s->plan;
-  std::vector<double> hu, hv;
   if (x || v) {
-    hu.resize(3 * (size_t)N);
-    hv.resize(3 * (size_t)N);
-    CI_CUDA(cudaMemcpyAsync(hu.data(), s->d_u.p, sizeof(double) * hu.size(), cudaMemcpyDeviceToHost,
-                            s->stream));
-    CI_CUDA(cudaMemcpyAsync(hv.data(), s->d_v.p, sizeof(double) * hv.size(), cudaMemcpyDeviceToHost,
-                            s->stream));
+    // permuted to the caller's order on the GPU, then one copy per array
+    int rc = ensure_exchange(s);
+    if (rc) return rc;
+    k_state_to_caller<<<(N + 255) / 256, 256, 0, s->stream>>>(
+        s->d_u.p, s->d_v.p, s->d_Xc.p, s->d_node_new.p, N, x ? s->d_xc.p : nullptr,
+        v ? s->d_vc.p : nullptr);
+    CI_CUDA(cudaGetLastError());
+    if (x)
+      CI_CUDA(cudaMemcpyAsync(x, s->d_xc.p, sizeof(double) * 3 * (size_t)N, cudaMemcpyDeviceToHost,
+                              s->stream));
+    if (v)
+      CI_CUDA(cudaMemcpyAsync(v, s->d_vc.p, sizeof(double) * 3 * (size_t)N, cudaMemcpyDeviceToHost,
+                              s->stream));
   }
   std::vector<float> hm, hep;
   std::vector<float4> hsa;
@@ -811,15 +870,12 @@ int ci_get_state(ci_solver* s, double* x, double* v, double* mass, float* sigma,
     CI_CUDA(cudaMemcpyAsync(hc.data(), s->d_contact.p, N, cudaMemcpyDeviceToHost, s->stream));
   }
   CI_CUDA(cudaStreamSynchronize(s->stream));
-  for (int i = 0; i < N; i++) {
-    const int n = P.node_orig[i];
-    for (int k = 0; k < 3; k++) {
-      if (x) x[3 * (size_t)n + k] = s->X[3 * (size_t)n + k] + hu[(size_t)k * N + i];
-      if (v) v[3 * (size_t)n + k] = hv[(size_t)k * N + i];
+  if (mass || contact)
+    for (int i = 0; i < N; i++) {
+      const int n = P.node_orig[i];
+      if (mass) mass[n] = hm[i];
+      if (contact) contact[n] = hc[i];
     }
-    if (mass) mass[n] = hm[i];
-    if (contact) contact[n] = hc[i];
-  }
   for (int pe = 0; pe < E; pe++) {
     const int oe = P.elem_orig[pe];
     for (int q = 0; q < nq; q++) {
@@ -840,19 +896,15 @@ int ci_set_state(ci_solver* s, const double* x, const double* v) {
   if (!s || !x || !v) return fail(CI_ERR_INVALID, "null argument");
   CI_CUDA(cudaSetDevice(s->device));
   const int N = s->N;
-  const ci::Plan& P = s->plan;
-  std::vector<double> hu(3 * (size_t)N), hv(3 * (size_t)N);
-  for (int i = 0; i < N; i++) {
-    const int n = P.node_orig[i];
-    for (int k = 0; k < 3; k++) {
-      hu[(size_t)k * N + i] = x[3 * (size_t)n + k] - s->X[3 * (size_t)n + k];
-      hv[(size_t)k * N + i] = v[3 * (size_t)n + k];
-    }
-  }
-  CI_CUDA(cudaMemcpyAsync(s->d_u.p, hu.data(), sizeof(double) * hu.size(), cudaMemcpyHostToDevice,
+  int rc = ensure_exchange(s);
+  if (rc) return rc;
+  CI_CUDA(cudaMemcpyAsync(s->d_xc.p, x, sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice,
                           s->stream));
-  CI_CUDA(cudaMemcpyAsync(s->d_v.p, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice,
+  CI_CUDA(cudaMemcpyAsync(s->d_vc.p, v, sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice,
                           s->stream));
+  k_state_from_caller<<<(N + 255) / 256, 256, 0, s->stream>>>(s->d_xc.p, s->d_vc.p, s->d_Xc.p,
+                                                              s->d_node_new.p, N, s->d_u.p, s->d_v.p);
+  CI_CUDA(cudaGetLastError());
   CI_CUDA(cudaStreamSynchronize(s->stream));
   return CI_OK;
 }
@@ -918,6 +970,7 @@ int ci_load_state(ci_solver* s, const char* path) {
     return fail(CI_ERR_IO, "state file: truncated");
   s->X = X;
   s->vel0 = vel0;
+  s->xc_stale = true;
   int rc = upload_reference(s);
   if (rc) return rc;
   destroy_graph(s);
