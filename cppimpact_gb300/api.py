@@ -268,6 +268,14 @@ class Solver:
         out = dict(x=x, v=v, mass=m, sigma=sg, epbar=ep, contact=ct)
         return {k: val for k, val in out.items() if k in want}
 
+    def get_xv(self, x_out, v_out):
+        """Positions and velocities into caller-owned float64 [N, 3] arrays (no
+        allocation; pinned host arrays make the copies direct DMA)."""
+        for a in (x_out, v_out):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != 3 * self.N:
+                raise ValueError("x_out / v_out must be C-contiguous float64 with 3N entries")
+        check(lib().ci_get_state(self._h, _d(x_out), _d(v_out), None, None, None, None))
+
     def set_state(self, x, v):
         x = np.ascontiguousarray(x, dtype=np.float64)
         v = np.ascontiguousarray(v, dtype=np.float64)
