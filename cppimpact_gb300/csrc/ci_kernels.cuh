@@ -17,6 +17,7 @@
 #pragma once
 #include <cstdint>
 
+#include "ci_fpconv.h"
 #include "ci_plan.h"
 
 namespace ci {
@@ -544,14 +545,14 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     un[k] = __fma_rn(p.dt, v[k], u[k]);
-    uf[k] = (float)un[k];
+    uf[k] = f64_to_f32(un[k]);
   }
   // |d32 - d| <= 2^-22 (|d0| + |u|_1) for |n_k| <= 1; 1e-6 (1 + ...) covers it
   const float d32 = __fadd_rn(d0f, __fadd_rn(__fmul_rn(p.nf[0], uf[0]),
                                   __fadd_rn(__fmul_rn(p.nf[1], uf[1]), __fmul_rn(p.nf[2], uf[2]))));
   const float margin = 1e-6f * (1.f + fabsf(d0f) + fabsf(uf[0]) + fabsf(uf[1]) + fabsf(uf[2]));
   in_contact = false;
-  double ad[3] = {(double)a[0], (double)a[1], (double)a[2]};
+  double ad[3] = {f32_to_f64(a[0]), f32_to_f64(a[1]), f32_to_f64(a[2])};
   if (!(d32 > margin)) {
     const double d = __fma_rn(p.wall_n[2], un[2], __fma_rn(p.wall_n[1], un[1],
                               __fma_rn(p.wall_n[0], un[0], d0[g])));
@@ -561,7 +562,7 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         ad[k] = __fma_rn(c, p.wall_n[k], ad[k]);
-        a[k] = (float)ad[k];
+        a[k] = f64_to_f32(ad[k]);
       }
     }
   }
@@ -570,14 +571,15 @@ __device__ __forceinline__ void node_step(const NodeParams& p, float fx, float f
     v[k] = __fma_rn(p.dt, ad[k], v[k]);
     u[k] = un[k];
     uf_out[k] = uf[k];
-    vf_out[k] = (float)v[k];
+    vf_out[k] = f64_to_f32(v[k]);
   }
 }
 
 __device__ __forceinline__ void store_node(const FusedArgs& A, double* const (&uo)[3],
                                            double* const (&vo)[3], int g, const double (&u)[3],
                                            const double (&v)[3], const float (&vf)[3],
-                                           const float (&a)[3], bool in_contact, bool store_acc) {
+                                           const float (&a)[3], bool in_contact, bool store_acc,
+                                           unsigned char old) {
   bool finite = true;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
@@ -587,7 +589,6 @@ __device__ __forceinline__ void store_node(const FusedArgs& A, double* const (&u
     if (store_acc) A.acc[k][g] = a[k];
   }
   if (!finite) atomicOr(A.status, (unsigned)ST_NONFINITE);
-  const unsigned char old = A.contact[g];
   const unsigned char flag = in_contact ? 3 : (old & 2);
   if (flag != old) A.contact[g] = flag;
 }
@@ -630,24 +631,27 @@ __device__ __forceinline__ Tile make_tile(float* sm, int L) {
 
 // Stage S^n of every local node of the chunk in shared memory (x relative to the
 // chunk origin, dt v): completed from S^{n-1} and the previous halo (the owner stores
-// it), or read as it is on the first step of a call.
+// it), or read as it is on the first step of a call.  All of a node's loads (slot
+// range, halo slots, state, mass, wall distance, contact flag, reference position) are
+// issued before its update and stores.
 template <int BS>
 __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams& ep,
                                             const NodeParams& np, const ChunkInfo& ch,
-                                            int state_final, const Tile& T) {
+                                            int state_final, const Tile& T, int tid) {
   const DevPlan& P = A.P;
   const int L = ch.n_local;
-#pragma unroll 2
-  for (int l = threadIdx.x; l < L; l += BS) {
+  for (int l = tid; l < L; l += BS) {
     const int lb = ch.local_begin + l;
     const bool own = l < ch.n_own;
     const int g = own ? ch.own_begin + l : P.local_gid[lb];
-    float uf[3], vf[3];
+    float x0[3], uf[3], vf[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) x0[k] = P.local_x0[k * (size_t)P.Lt + lb];
     if (state_final) {
 #pragma unroll
       for (int k = 0; k < 3; k++) {
-        uf[k] = (float)A.u_cur[k][g];
-        vf[k] = (float)A.v_cur[k][g];
+        uf[k] = f64_to_f32(A.u_cur[k][g]);
+        vf[k] = f64_to_f32(A.v_cur[k][g]);
       }
     } else {
       // interior nodes: one slot at a known position; others: their node's slot range
@@ -660,14 +664,31 @@ __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams
         s0 = r.x;
         s1 = r.y;
       }
+      // slot sum in slot order starting from 0 (s1 > s0: the node's slot in this chunk)
+      const bool two = s1 > s0 + 1;
+      float f[3];
       double u[3], v[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const float h0 = A.halo_prv[k][s0];
+        const float h1 = two ? A.halo_prv[k][s0 + 1] : 0.f;
+        f[k] = __fadd_rn(0.f, h0);
+        if (two) f[k] = __fadd_rn(f[k], h1);
+        u[k] = A.u_prv[k][g];
+        v[k] = A.v_prv[k][g];
+      }
+      const float m = A.mass[g], d0f = A.d0f[g];
+      const unsigned char ct = A.contact[g];
+      for (int sl = s0 + 2; sl < s1; sl++) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) f[k] = __fadd_rn(f[k], A.halo_prv[k][sl]);
+      }
       float a[3];
       bool hit;
-      complete_node(A, np, g, s0, s1, u, v, a, hit, uf, vf);
-      if (own) store_node(A, A.u_cur, A.v_cur, g, u, v, vf, a, hit, false);
+      node_step(np, f[0], f[1], f[2], m, d0f, A.d0, g, u, v, a, hit, uf, vf);
+      if (own) store_node(A, A.u_cur, A.v_cur, g, u, v, vf, a, hit, false, ct);
     }
-    T.p0[l] = make_float4(P.local_x0[lb] + uf[0], P.local_x0[(size_t)P.Lt + lb] + uf[1],
-                          P.local_x0[2 * (size_t)P.Lt + lb] + uf[2], ep.dt * vf[0]);
+    T.p0[l] = make_float4(x0[0] + uf[0], x0[1] + uf[1], x0[2] + uf[2], ep.dt * vf[0]);
     T.p1[l] = make_float2(ep.dt * vf[1], ep.dt * vf[2]);
     T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
@@ -676,11 +697,11 @@ __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams
 // Every local node's partial force of this step to its slot in the halo.
 template <int BS>
 __device__ __forceinline__ void node_epilogue(const FusedArgs& A, const ChunkInfo& ch,
-                                              const Tile& T) {
+                                              const Tile& T, int tid) {
   const DevPlan& P = A.P;
   const int L = ch.n_local;
 #pragma unroll 4
-  for (int l = threadIdx.x; l < L; l += BS) {
+  for (int l = tid; l < L; l += BS) {
     const float4 f = T.acc[l];
     const int s = l < ch.n_int ? ch.slot_begin + l : P.local_slot[ch.local_begin + l];
     A.halo_cur[0][s] = f.x;
@@ -689,12 +710,38 @@ __device__ __forceinline__ void node_epilogue(const FusedArgs& A, const ChunkInf
   }
 }
 
+// Barrier over a thread group of n threads: id 0 is the whole CTA (the only group of the
+// current kernels; named barriers 1..15 would serve sub-CTA groups).
+__device__ __forceinline__ void group_sync(int id, int n) {
+  if (id == 0)
+    __syncthreads();
+  else
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+// Sum over a group of BS threads (tid = index in the group); the result is valid on tid 0.
 template <int BS>
-__device__ __forceinline__ void add_chunk_work(const FusedArgs& A, float wint, float wp, float* red) {
-  const float t0 = block_sum<BS>(wint, red);
-  const float t1 = block_sum<BS>(wp, red);
-  if (threadIdx.x == 0) {
-    double* cw = A.chunk_work + 4 * (size_t)blockIdx.x;
+__device__ __forceinline__ float group_sum(float v, float* red, int tid, int bar) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = tid >> 5, l = tid & 31;
+  group_sync(bar, BS);
+  if (l == 0) red[w] = v;
+  group_sync(bar, BS);
+  float t = 0.f;
+  if (tid == 0)
+    for (int k = 0; k < BS / 32; k++) t += red[k];
+  return t;
+}
+
+// The group's internal and plastic work of this step added to chunk c's running sums.
+template <int BS>
+__device__ __forceinline__ void add_chunk_work(const FusedArgs& A, int c, float wint, float wp,
+                                               float* red, int tid, int bar) {
+  const float t0 = group_sum<BS>(wint, red, tid, bar);
+  const float t1 = group_sum<BS>(wp, red, tid, bar);
+  if (tid == 0) {
+    double* cw = A.chunk_work + 4 * (size_t)c;
     cw[0] += (double)t0;
     cw[1] += (double)t1;
   }
@@ -714,7 +761,7 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, Nod
   const Tile T = make_tile(sm, L);
   __shared__ float red[BS / 32];
 
-  stage_nodes<BS>(A, ep, np, ch, cs.state_final, T);
+  stage_nodes<BS>(A, ep, np, ch, cs.state_final, T, threadIdx.x);
   if (cs.mode == 1) return;
   __syncthreads();
 
@@ -765,8 +812,8 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, Nod
     }
   }
   __syncthreads();
-  node_epilogue<BS>(A, ch, T);
-  if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
+  node_epilogue<BS>(A, ch, T, threadIdx.x);
+  if (ep.accum_energy) add_chunk_work<BS>(A, blockIdx.x, wint, wp, red, threadIdx.x, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -878,32 +925,22 @@ __device__ __forceinline__ void tet10_rs_slot(const Tet10QP& t, const float (&Pm
   R[K] = (even ? m0 : m1) + __shfl_xor_sync(0xffffffffu, even ? m1 : m0, 1);
 }
 
-// 6 CTAs of 128 threads per SM (80 registers) fit the 896-node chunk's shared tile
-template <int MODE, int BS, bool BATCH = false>
-__global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
-  extern __shared__ float sm[];
+// Element loop of one chunk by a group of BS threads (4 lanes per element, colours
+// applied in order between group barriers), then the chunk's partial nodal forces to the
+// halo and its work to chunk c's sums.
+template <int MODE, int BS>
+__device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const ElemParams& ep,
+                                                   const ChunkInfo& ch, const Tile& T, int tid,
+                                                   int bar, int c, float* red) {
   const DevPlan& P = A.P;
-  const ChunkInfo ch = P.chunks[blockIdx.x];
-  const ChunkStep cs = chunk_step<BATCH>(A, ch, ep_arg, np_arg);
-  if (cs.mode == 2) return;
-  const ElemParams& ep = cs.ep;
-  const NodeParams& np = cs.np;
-  const int L = ch.n_local;
-  const Tile T = make_tile(sm, L);
-  __shared__ float red[BS / 32];
-
-  stage_nodes<BS>(A, ep, np, ch, cs.state_final, T);
-  if (cs.mode == 1) return;
-  __syncthreads();
-
-  const int q = threadIdx.x & 3;
+  const int q = tid & 3;
   const Tet10QP t = tet10_qp(q);
   constexpr float W = 1.0f / 24.0f;
   const int E = P.E;
   float wint = 0.f, wp = 0.f;
   constexpr int EPW = BS / 4;  // elements per window
   for (int w = ch.elem_begin; w < ch.elem_end; w += EPW) {
-    const int e = w + (threadIdx.x >> 2);
+    const int e = w + (tid >> 2);
     const bool act = e < ch.elem_end;
     const int ee = act ? e : ch.elem_begin;  // inactive lanes shadow a valid element
     int ln[10];
@@ -1000,7 +1037,7 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
     const int c0 = P.color[w];
     const int c1 = P.color[min(w + EPW, ch.elem_end) - 1];
     for (int k = c0; k <= c1; k++) {
-      __syncthreads();
+      group_sync(bar, BS);
       if (col == k) {
         float4 t0 = T.acc[own0];
         t0.x += keep[0][0];
@@ -1022,9 +1059,26 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
       }
     }
   }
+  group_sync(bar, BS);
+  node_epilogue<BS>(A, ch, T, tid);
+  if (ep.accum_energy) add_chunk_work<BS>(A, c, wint, wp, red, tid, bar);
+}
+
+// 6 CTAs of 128 threads per SM (80 registers) fit the 896-node chunk's shared tile
+template <int MODE, int BS, bool BATCH = false>
+__global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
+  extern __shared__ float sm[];
+  const DevPlan& P = A.P;
+  const ChunkInfo ch = P.chunks[blockIdx.x];
+  const ChunkStep cs = chunk_step<BATCH>(A, ch, ep_arg, np_arg);
+  if (cs.mode == 2) return;
+  const Tile T = make_tile(sm, ch.n_local);
+  __shared__ float red[BS / 32];
+
+  stage_nodes<BS>(A, cs.ep, cs.np, ch, cs.state_final, T, threadIdx.x);
+  if (cs.mode == 1) return;
   __syncthreads();
-  node_epilogue<BS>(A, ch, T);
-  if (ep.accum_energy) add_chunk_work<BS>(A, wint, wp, red);
+  step_qp10_elements<MODE, BS>(A, cs.ep, ch, T, threadIdx.x, 0, blockIdx.x, red);
 }
 
 // S^N of every node after the last fused step of a call: reads S^{N-1} from the prv
@@ -1036,7 +1090,7 @@ static __global__ void __launch_bounds__(256) k_finalize_nodes(FusedArgs A, Node
   float a[3], uf[3], vf[3];
   bool hit;
   complete_node(A, np, g, A.P.slot_row[g], A.P.slot_row[g + 1], u, v, a, hit, uf, vf);
-  store_node(A, A.u_cur, A.v_cur, g, u, v, vf, a, hit, A.store_acc != 0);
+  store_node(A, A.u_cur, A.v_cur, g, u, v, vf, a, hit, A.store_acc != 0, A.contact[g]);
 }
 
 // a0 from zero internal force (wall at the start positions, gravity) and the half step
