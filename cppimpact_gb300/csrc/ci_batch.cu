@@ -201,6 +201,8 @@ cudaError_t launch_batch_bs(Group& G, const FusedArgs& F) {
   const NodeParams np{};
   if (NPE == 10 && G.elem_lanes == 4)
     k_step_qp10<EM_J2, BS, true><<<G.C, BS, G.smem, G.stream>>>(F, ep, np);
+  else if (NPE == 10)
+    k_step_t10<EM_J2, BS, true><<<G.C, BS, G.smem, G.stream>>>(F, ep, np);
   else
     k_step<NPE, EM_J2, BS, true><<<G.C, BS, G.smem, G.stream>>>(F, ep, np);
   return cudaGetLastError();
@@ -219,10 +221,14 @@ cudaError_t configure_bs(int bytes) {
   if ((e = cudaFuncSetAttribute(k_step<NPE, EM_J2, BS, true>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
     return e;
-  if (NPE == 10)
+  if (NPE == 10) {
     if ((e = cudaFuncSetAttribute(k_step_qp10<EM_J2, BS, true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
       return e;
+    if ((e = cudaFuncSetAttribute(k_step_t10<EM_J2, BS, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+      return e;
+  }
   return cudaFuncSetAttribute(k_elem<NPE, EM_MASS_HRZ, 256>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }

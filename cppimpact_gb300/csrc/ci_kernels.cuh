@@ -1081,6 +1081,231 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
   step_qp10_elements<MODE, BS>(A, cs.ep, ch, T, threadIdx.x, 0, blockIdx.x, red);
 }
 
+// ---------------------------------------------------------------------------
+// tet10, one thread per element, all four Gauss points, in barycentric form.
+//
+// With g_0 = e_xi, g_1 = e_eta, g_2 = -(1,1,1), g_3 = e_zeta the gradients of the
+// barycentrics, corner k has grad N_k = (A_k - 1) g_k and edge (k,l) has
+// grad N_kl = A_l g_k + A_k g_l (A = 4L).  At Gauss point p one barycentric is a and
+// the other three b (corner kappa(p) = 2, 0, 1, 3 for p = 0..3), so A_m = 4b + 4(a-b)
+// [m == kappa].  Hence
+//   J_p = sum_k C_k g_k^T,  C_k = Y_k + 4(a-b) (k == kappa ? x_kappa : x_{k,kappa}),
+//   Y_k = (4b-1) x_k + 4b sum_{l != k} x_{kl}       (the same at every point),
+// and with Q_k(p) = P_p g_k (P = w detJ sigma J^-T) the element forces are
+//   f_k  = (4b-1) S_k + 4(a-b) Q_k(p(k)),
+//   f_kl = 4b (S_k + S_l) + 4(a-b) (Q_k(p(l)) + Q_l(p(k))),   S_k = sum_p Q_k(p),
+// where p(k) is the point at which corner k carries the weight a.  Every index is
+// known at compile time: about half the arithmetic of the per-node sums, no shuffles.
+// ---------------------------------------------------------------------------
+// edge node of corners k != l (CalculiX order 4:(0,1) 5:(1,2) 6:(2,0) 7:(0,3) 8:(1,3) 9:(2,3))
+__device__ __host__ __forceinline__ constexpr int t10_edge(int k, int l) {
+  const int lo = k < l ? k : l, hi = k < l ? l : k;
+  return lo == 0 ? (hi == 1 ? 4 : hi == 2 ? 6 : 7) : lo == 1 ? (hi == 2 ? 5 : 8) : 9;
+}
+__device__ __host__ __forceinline__ constexpr int t10_kappa(int p) { return p == 0 ? 2 : p == 1 ? 0 : p == 2 ? 1 : 3; }
+
+template <int MODE>
+__device__ __forceinline__ void tet10_bary_element(const ElemParams& ep, const FusedArgs& A, int e,
+                                                   const Tile& T, const int (&ln)[10],
+                                                   float (&F)[10][3], float& wint, float& wp) {
+  constexpr float qa = 0.58541019662496845f, qb = 0.13819660112501052f;
+  constexpr float AL = 4.f * qb - 1.f, BE = 4.f * qb, GA = 4.f * (qa - qb);
+  constexpr float W = 1.0f / 24.0f;
+  // Y_k for positions (Yx) and increments (Yd), corners k = 0..3
+  float Yx[4][3], Yd[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const float4 q0 = T.p0[ln[k]];
+    const float2 q1 = T.p1[ln[k]];
+    Yx[k][0] = AL * q0.x; Yx[k][1] = AL * q0.y; Yx[k][2] = AL * q0.z;
+    Yd[k][0] = AL * q0.w; Yd[k][1] = AL * q1.x; Yd[k][2] = AL * q1.y;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+#pragma unroll
+    for (int l = k + 1; l < 4; l++) {
+      const int m = t10_edge(k, l);
+      const float4 q0 = T.p0[ln[m]];
+      const float2 q1 = T.p1[ln[m]];
+      const float xs[3] = {q0.x, q0.y, q0.z}, ds[3] = {q0.w, q1.x, q1.y};
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        Yx[k][c] = fmaf(BE, xs[c], Yx[k][c]);
+        Yx[l][c] = fmaf(BE, xs[c], Yx[l][c]);
+        Yd[k][c] = fmaf(BE, ds[c], Yd[k][c]);
+        Yd[l][c] = fmaf(BE, ds[c], Yd[l][c]);
+      }
+    }
+  float Sq[3][3];  // S_k for k = 0, 1, 3 (rows), component c
+#pragma unroll
+  for (int i = 0; i < 3; i++) Sq[i][0] = Sq[i][1] = Sq[i][2] = 0.f;
+#pragma unroll
+  for (int i = 0; i < 10; i++) F[i][0] = F[i][1] = F[i][2] = 0.f;
+#pragma unroll
+  for (int p = 0; p < 4; p++) {
+    const int kap = t10_kappa(p);
+    // C_k = Y_k + GA * (point node of k at p)
+    float Cx[4][3], Cd[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int m = k == kap ? k : t10_edge(k, kap);
+      const float4 q0 = T.p0[ln[m]];
+      const float2 q1 = T.p1[ln[m]];
+      Cx[k][0] = fmaf(GA, q0.x, Yx[k][0]);
+      Cx[k][1] = fmaf(GA, q0.y, Yx[k][1]);
+      Cx[k][2] = fmaf(GA, q0.z, Yx[k][2]);
+      Cd[k][0] = fmaf(GA, q0.w, Yd[k][0]);
+      Cd[k][1] = fmaf(GA, q1.x, Yd[k][1]);
+      Cd[k][2] = fmaf(GA, q1.y, Yd[k][2]);
+    }
+    float J[9], Gu[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      J[3 * a + 0] = Cx[0][a] - Cx[2][a];
+      J[3 * a + 1] = Cx[1][a] - Cx[2][a];
+      J[3 * a + 2] = Cx[3][a] - Cx[2][a];
+      Gu[3 * a + 0] = Cd[0][a] - Cd[2][a];
+      Gu[3 * a + 1] = Cd[1][a] - Cd[2][a];
+      Gu[3 * a + 2] = Cd[3][a] - Cd[2][a];
+    }
+    float Ji[9];
+    const float detJ = inv3f(J, Ji);
+    if (!(detJ > 0.f)) atomicOr(A.status, (unsigned)ST_DEGENERATE);
+    const float wd = W * detJ;
+    float Lg[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++)
+        Lg[3 * a + b] = Gu[3 * a + 0] * Ji[0 * 3 + b] + Gu[3 * a + 1] * Ji[1 * 3 + b] +
+                        Gu[3 * a + 2] * Ji[2 * 3 + b];
+    const float de[6] = {Lg[0], Lg[4], Lg[8], Lg[1] + Lg[3], Lg[5] + Lg[7], Lg[2] + Lg[6]};
+    const float tr = de[0] + de[1] + de[2];
+    float s[6];
+    if (MODE == EM_REFCOMPAT) {
+      s[0] = ep.lambda * tr + 2.f * ep.mu * de[0];
+      s[1] = ep.lambda * tr + 2.f * ep.mu * de[1];
+      s[2] = ep.lambda * tr + 2.f * ep.mu * de[2];
+      s[3] = ep.mu * de[3];
+      s[4] = ep.mu * de[4];
+      s[5] = ep.mu * de[5];
+      if (ep.accum_energy) {
+        float w = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; k++) w = fmaf(s[k], de[k], w);
+        wint = fmaf(0.5f * wd, w, wint);
+      }
+    } else {
+      const size_t qi = (size_t)e * 4 + p;
+      const float4 sa = A.sig_a[qi];
+      const float2 sb = A.sig_b[qi];
+      const float ep0 = A.epbar[qi];
+      const float s0[6] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y};
+      s[0] = s0[0] + ep.lambda * tr + 2.f * ep.mu * de[0];
+      s[1] = s0[1] + ep.lambda * tr + 2.f * ep.mu * de[1];
+      s[2] = s0[2] + ep.lambda * tr + 2.f * ep.mu * de[2];
+      s[3] = s0[3] + ep.mu * de[3];
+      s[4] = s0[4] + ep.mu * de[4];
+      s[5] = s0[5] + ep.mu * de[5];
+      float epn = ep0;
+      j2_return(ep, s, epn);
+      A.sig_a[qi] = make_float4(s[0], s[1], s[2], s[3]);
+      A.sig_b[qi] = make_float2(s[4], s[5]);
+      A.epbar[qi] = epn;
+      if (ep.accum_energy) {
+        float w = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; k++) w = fmaf(s0[k] + s[k], de[k], w);
+        wint = fmaf(0.5f * wd, w, wint);
+        wp = fmaf(wd * (ep.sy0 + ep.H * epn), epn - ep0, wp);
+      }
+    }
+    const float Sg[9] = {s[0], s[3], s[5], s[3], s[1], s[4], s[5], s[4], s[2]};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      float Pr[3];  // row c of P
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        Pr[j] = wd * (Sg[3 * c + 0] * Ji[3 * j + 0] + Sg[3 * c + 1] * Ji[3 * j + 1] +
+                      Sg[3 * c + 2] * Ji[3 * j + 2]);
+      // Q_k = P g_k: Q_0 = P_0, Q_1 = P_1, Q_3 = P_2, Q_2 = -(P_0 + P_1 + P_2)
+      const float Q[4] = {Pr[0], Pr[1], -(Pr[0] + Pr[1] + Pr[2]), Pr[2]};
+      Sq[0][c] += Q[0];
+      Sq[1][c] += Q[1];
+      Sq[2][c] += Q[3];
+      // the point terms of this point: corner kappa and the edges (kappa, l)
+      F[kap][c] = fmaf(GA, Q[kap], F[kap][c]);
+#pragma unroll
+      for (int l = 0; l < 4; l++)
+        if (l != kap) F[t10_edge(kap, l)][c] = fmaf(GA, Q[l], F[t10_edge(kap, l)][c]);
+    }
+  }
+  // the smooth terms: corners (4b-1) S_k, edges 4b (S_k + S_l)
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const float S[4] = {Sq[0][c], Sq[1][c], -(Sq[0][c] + Sq[1][c] + Sq[2][c]), Sq[2][c]};
+#pragma unroll
+    for (int k = 0; k < 4; k++) F[k][c] = fmaf(AL, S[k], F[k][c]);
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int l = k + 1; l < 4; l++)
+        F[t10_edge(k, l)][c] = fmaf(BE, S[k] + S[l], F[t10_edge(k, l)][c]);
+  }
+}
+
+// Fused tet10 step, one thread per element (tet10_bary_element).  4 CTAs of 128
+// threads per SM (at most 128 registers).
+template <int MODE, int BS, bool BATCH = false>
+__global__ void __launch_bounds__(BS, 512 / BS) k_step_t10(FusedArgs A, ElemParams ep_arg, NodeParams np_arg) {
+  extern __shared__ float sm[];
+  const DevPlan& P = A.P;
+  const ChunkInfo ch = P.chunks[blockIdx.x];
+  const ChunkStep cs = chunk_step<BATCH>(A, ch, ep_arg, np_arg);
+  if (cs.mode == 2) return;
+  const ElemParams& ep = cs.ep;
+  const Tile T = make_tile(sm, ch.n_local);
+  __shared__ float red[BS / 32];
+
+  stage_nodes<BS>(A, ep, cs.np, ch, cs.state_final, T, threadIdx.x);
+  if (cs.mode == 1) return;
+  __syncthreads();
+
+  float wint = 0.f, wp = 0.f;
+  const int E = P.E;
+  for (int w = ch.elem_begin; w < ch.elem_end; w += BS) {
+    const int e = w + threadIdx.x;
+    const bool act = e < ch.elem_end;
+    int col = -1;
+    int ln[10];
+    float f[10][3];
+    if (act) {
+      col = P.color[e];
+#pragma unroll
+      for (int a = 0; a < 10; a++) ln[a] = P.conn_local[(size_t)a * E + e];
+      tet10_bary_element<MODE>(ep, A, e, T, ln, f, wint, wp);
+    }
+    const int c0 = P.color[w];
+    const int c1 = P.color[min(w + BS, ch.elem_end) - 1];
+    for (int k = c0; k <= c1; k++) {
+      __syncthreads();
+      if (col == k) {
+#pragma unroll
+        for (int a = 0; a < 10; a++) {
+          float4 t = T.acc[ln[a]];
+          t.x += f[a][0];
+          t.y += f[a][1];
+          t.z += f[a][2];
+          T.acc[ln[a]] = t;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  node_epilogue<BS>(A, ch, T, threadIdx.x);
+  if (ep.accum_energy) add_chunk_work<BS>(A, blockIdx.x, wint, wp, red, threadIdx.x, 0);
+}
+
 // S^N of every node after the last fused step of a call: reads S^{N-1} from the prv
 // buffer and the halo of step N-1, writes S^N (and a^N) to the cur buffer.
 static __global__ void __launch_bounds__(256) k_finalize_nodes(FusedArgs A, NodeParams np) {

@@ -246,6 +246,12 @@ cudaError_t configure_step(int bytes) {
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e) return e;
   if (NPE == 10) {
+    if ((e = cudaFuncSetAttribute(ci::k_step_t10<ci::EM_J2, BS>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+      return e;
+    if ((e = cudaFuncSetAttribute(ci::k_step_t10<ci::EM_REFCOMPAT, BS>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+      return e;
     if ((e = cudaFuncSetAttribute(ci::k_step_qp10<ci::EM_J2, BS>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
       return e;
@@ -286,6 +292,13 @@ cudaError_t launch_fused_bs(ci_solver* s, const ci::FusedArgs& F, const ci::Elem
       ci::k_step_qp10<ci::EM_J2, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
     else
       ci::k_step_qp10<ci::EM_REFCOMPAT, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
+    return cudaGetLastError();
+  }
+  if (NPE == 10) {
+    if (s->opt.mode != CI_MODE_REFCOMPAT)
+      ci::k_step_t10<ci::EM_J2, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
+    else
+      ci::k_step_t10<ci::EM_REFCOMPAT, BS><<<s->C, BS, s->smem_bytes, s->stream>>>(F, ep, np);
     return cudaGetLastError();
   }
   if (s->opt.mode != CI_MODE_REFCOMPAT)
