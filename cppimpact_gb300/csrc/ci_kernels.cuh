@@ -694,6 +694,77 @@ __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams
   }
 }
 
+// stage_nodes with K nodes per thread in flight: the loads of K nodes are issued before
+// the first of their updates (for kernels with registers to spare during the staging).
+template <int BS, int K>
+__device__ __forceinline__ void stage_nodes_k(const FusedArgs& A, const ElemParams& ep,
+                                              const NodeParams& np, const ChunkInfo& ch,
+                                              int state_final, const Tile& T, int tid) {
+  if (K == 1 || state_final) {
+    stage_nodes<BS>(A, ep, np, ch, state_final, T, tid);
+    return;
+  }
+  const DevPlan& P = A.P;
+  const int L = ch.n_local;
+  for (int l0 = tid; l0 < L; l0 += K * BS) {
+    int g[K], s0[K], s1[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+      const int l = min(l0 + j * BS, L - 1);  // past the end: repeat the last node, unused
+      const int lb = ch.local_begin + l;
+      g[j] = l < ch.n_own ? ch.own_begin + l : P.local_gid[lb];
+      if (l < ch.n_int) {
+        s0[j] = ch.slot_begin + l;
+        s1[j] = s0[j] + 1;
+      } else {
+        const int2 r = P.local_srow[lb];
+        s0[j] = r.x;
+        s1[j] = r.y;
+      }
+    }
+    float f[K][3], m[K], d0f[K], x0[K][3];
+    double u[K][3], v[K][3];
+    unsigned char ct[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+      const size_t lb = ch.local_begin + min(l0 + j * BS, L - 1);
+      const bool two = s1[j] > s0[j] + 1;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const float h0 = A.halo_prv[k][s0[j]];
+        const float h1 = two ? A.halo_prv[k][s0[j] + 1] : 0.f;
+        f[j][k] = __fadd_rn(0.f, h0);
+        if (two) f[j][k] = __fadd_rn(f[j][k], h1);
+        u[j][k] = A.u_prv[k][g[j]];
+        v[j][k] = A.v_prv[k][g[j]];
+        x0[j][k] = P.local_x0[k * (size_t)P.Lt + lb];
+      }
+      m[j] = A.mass[g[j]];
+      d0f[j] = A.d0f[g[j]];
+      ct[j] = A.contact[g[j]];
+    }
+#pragma unroll
+    for (int j = 0; j < K; j++)
+      for (int sl = s0[j] + 2; sl < s1[j]; sl++) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) f[j][k] = __fadd_rn(f[j][k], A.halo_prv[k][sl]);
+      }
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+      const int l = l0 + j * BS;
+      if (l >= L) break;
+      float a[3], uf[3], vf[3];
+      bool hit;
+      node_step(np, f[j][0], f[j][1], f[j][2], m[j], d0f[j], A.d0, g[j], u[j], v[j], a, hit, uf,
+                vf);
+      if (l < ch.n_own) store_node(A, A.u_cur, A.v_cur, g[j], u[j], v[j], vf, a, hit, false, ct[j]);
+      T.p0[l] = make_float4(x0[j][0] + uf[0], x0[j][1] + uf[1], x0[j][2] + uf[2], ep.dt * vf[0]);
+      T.p1[l] = make_float2(ep.dt * vf[1], ep.dt * vf[2]);
+      T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
 // Every local node's partial force of this step to its slot in the halo.
 template <int BS>
 __device__ __forceinline__ void node_epilogue(const FusedArgs& A, const ChunkInfo& ch,
@@ -1267,7 +1338,10 @@ __global__ void __launch_bounds__(BS, 512 / BS) k_step_t10(FusedArgs A, ElemPara
   const Tile T = make_tile(sm, ch.n_local);
   __shared__ float red[BS / 32];
 
-  stage_nodes<BS>(A, ep, cs.np, ch, cs.state_final, T, threadIdx.x);
+#ifndef CI_T10_STAGE_K
+#define CI_T10_STAGE_K 4
+#endif
+  stage_nodes_k<BS, CI_T10_STAGE_K>(A, ep, cs.np, ch, cs.state_final, T, threadIdx.x);
   if (cs.mode == 1) return;
   __syncthreads();
 
