@@ -781,37 +781,13 @@ __device__ __forceinline__ void node_epilogue(const FusedArgs& A, const ChunkInf
   }
 }
 
-// Barrier over a thread group of n threads: id 0 is the whole CTA (the only group of the
-// current kernels; named barriers 1..15 would serve sub-CTA groups).
-__device__ __forceinline__ void group_sync(int id, int n) {
-  if (id == 0)
-    __syncthreads();
-  else
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
-}
-
-// Sum over a group of BS threads (tid = index in the group); the result is valid on tid 0.
-template <int BS>
-__device__ __forceinline__ float group_sum(float v, float* red, int tid, int bar) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int w = tid >> 5, l = tid & 31;
-  group_sync(bar, BS);
-  if (l == 0) red[w] = v;
-  group_sync(bar, BS);
-  float t = 0.f;
-  if (tid == 0)
-    for (int k = 0; k < BS / 32; k++) t += red[k];
-  return t;
-}
-
-// The group's internal and plastic work of this step added to chunk c's running sums.
+// The CTA's internal and plastic work of this step added to chunk c's running sums.
 template <int BS>
 __device__ __forceinline__ void add_chunk_work(const FusedArgs& A, int c, float wint, float wp,
-                                               float* red, int tid, int bar) {
-  const float t0 = group_sum<BS>(wint, red, tid, bar);
-  const float t1 = group_sum<BS>(wp, red, tid, bar);
-  if (tid == 0) {
+                                               float* red) {
+  const float t0 = block_sum<BS>(wint, red);
+  const float t1 = block_sum<BS>(wp, red);
+  if (threadIdx.x == 0) {
     double* cw = A.chunk_work + 4 * (size_t)c;
     cw[0] += (double)t0;
     cw[1] += (double)t1;
@@ -884,7 +860,7 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, Nod
   }
   __syncthreads();
   node_epilogue<BS>(A, ch, T, threadIdx.x);
-  if (ep.accum_energy) add_chunk_work<BS>(A, blockIdx.x, wint, wp, red, threadIdx.x, 0);
+  if (ep.accum_energy) add_chunk_work<BS>(A, blockIdx.x, wint, wp, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -996,13 +972,13 @@ __device__ __forceinline__ void tet10_rs_slot(const Tet10QP& t, const float (&Pm
   R[K] = (even ? m0 : m1) + __shfl_xor_sync(0xffffffffu, even ? m1 : m0, 1);
 }
 
-// Element loop of one chunk by a group of BS threads (4 lanes per element, colours
-// applied in order between group barriers), then the chunk's partial nodal forces to the
-// halo and its work to chunk c's sums.
+// Element loop of one chunk by the CTA's BS threads (4 lanes per element, colours
+// applied in order between barriers), then the chunk's partial nodal forces to the halo
+// and its work to chunk c's sums.
 template <int MODE, int BS>
 __device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const ElemParams& ep,
                                                    const ChunkInfo& ch, const Tile& T, int tid,
-                                                   int bar, int c, float* red) {
+                                                   int c, float* red) {
   const DevPlan& P = A.P;
   const int q = tid & 3;
   const Tet10QP t = tet10_qp(q);
@@ -1108,7 +1084,7 @@ __device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const Ele
     const int c0 = P.color[w];
     const int c1 = P.color[min(w + EPW, ch.elem_end) - 1];
     for (int k = c0; k <= c1; k++) {
-      group_sync(bar, BS);
+      __syncthreads();
       if (col == k) {
         float4 t0 = T.acc[own0];
         t0.x += keep[0][0];
@@ -1130,9 +1106,9 @@ __device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const Ele
       }
     }
   }
-  group_sync(bar, BS);
+  __syncthreads();
   node_epilogue<BS>(A, ch, T, tid);
-  if (ep.accum_energy) add_chunk_work<BS>(A, c, wint, wp, red, tid, bar);
+  if (ep.accum_energy) add_chunk_work<BS>(A, c, wint, wp, red);
 }
 
 // 6 CTAs of 128 threads per SM (80 registers) fit the 896-node chunk's shared tile
@@ -1149,7 +1125,7 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
   stage_nodes<BS>(A, cs.ep, cs.np, ch, cs.state_final, T, threadIdx.x);
   if (cs.mode == 1) return;
   __syncthreads();
-  step_qp10_elements<MODE, BS>(A, cs.ep, ch, T, threadIdx.x, 0, blockIdx.x, red);
+  step_qp10_elements<MODE, BS>(A, cs.ep, ch, T, threadIdx.x, blockIdx.x, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -1377,7 +1353,7 @@ __global__ void __launch_bounds__(BS, 512 / BS) k_step_t10(FusedArgs A, ElemPara
   }
   __syncthreads();
   node_epilogue<BS>(A, ch, T, threadIdx.x);
-  if (ep.accum_energy) add_chunk_work<BS>(A, blockIdx.x, wint, wp, red, threadIdx.x, 0);
+  if (ep.accum_energy) add_chunk_work<BS>(A, blockIdx.x, wint, wp, red);
 }
 
 // S^N of every node after the last fused step of a call: reads S^{N-1} from the prv
