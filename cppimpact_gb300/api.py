@@ -88,6 +88,7 @@ EXPORTS = {
     "ci_steps_done": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "ci_get_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _fp, _fp, _ubp]),
     "ci_set_state": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "ci_deformation_gradient": (C.c_int, [C.c_void_p, _dp]),
     "ci_save_state": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ci_load_state": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ci_get_energy": (C.c_int, [C.c_void_p, C.POINTER(CiEnergy)]),
@@ -275,6 +276,13 @@ class Solver:
             if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != 3 * self.N:
                 raise ValueError("x_out / v_out must be C-contiguous float64 with 3N entries")
         check(lib().ci_get_state(self._h, _d(x_out), _d(v_out), None, None, None, None))
+
+    def deformation_gradient(self):
+        """F = I + du/dX at every Gauss point of the current state, float64 [E, nq, 3, 3]
+        in the caller's element order (ci_deformation_gradient)."""
+        F = np.zeros((self.E, self.nq, 3, 3))
+        check(lib().ci_deformation_gradient(self._h, _d(F)))
+        return F
 
     def set_state(self, x, v):
         x = np.ascontiguousarray(x, dtype=np.float64)

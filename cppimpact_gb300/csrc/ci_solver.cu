@@ -616,6 +616,67 @@ struct FileCloser {
 
 namespace {
 // x (caller AoS) = X + u (plan SoA), v likewise; one thread per caller node
+// Shape-function gradients in reference coordinates, FP64 (the element geometry of
+// Rule<NPE>: corners L = (xi, eta, 1-xi-eta-zeta, zeta), CalculiX edge order).
+template <int NPE>
+__device__ void ref_grad_f64(int q, double (&G)[NPE][3]) {
+  const double dL[4][3] = {{1, 0, 0}, {0, 1, 0}, {-1, -1, -1}, {0, 0, 1}};
+  if (NPE == 4) {
+    for (int c = 0; c < 4; c++)
+      for (int j = 0; j < 3; j++) G[c][j] = dL[c == 0 ? 2 : c == 1 ? 0 : c == 2 ? 1 : 3][j];
+    return;
+  }
+  const double a = 0.58541019662496845446, b = 0.13819660112501051518;
+  const double L[4] = {q == 1 ? a : b, q == 2 ? a : b, q == 0 ? a : b, q == 3 ? a : b};
+  const int ea[6] = {0, 1, 2, 0, 1, 2}, eb[6] = {1, 2, 0, 3, 3, 3};
+  for (int c = 0; c < 4; c++)
+    for (int j = 0; j < 3; j++) G[c][j] = (4 * L[c] - 1) * dL[c][j];
+  for (int k = 0; k < 6 && 4 + k < NPE; k++)
+    for (int j = 0; j < 3; j++)
+      G[4 + k][j] = 4 * (L[ea[k]] * dL[eb[k]][j] + L[eb[k]] * dL[ea[k]][j]);
+}
+
+// Deformation gradient F = I + du/dX at every Gauss point, FP64, plan order [E][nq][9]
+// (row a, column j: delta_aj + d u_a / d X_j); one CTA per chunk.
+template <int NPE>
+__global__ void __launch_bounds__(128) k_defgrad(ci::DevPlan P, const double* u0, const double* u1,
+                                                 const double* u2, int nq, double* F) {
+  const ci::ChunkInfo ch = P.chunks[blockIdx.x];
+  const int ne = ch.elem_end - ch.elem_begin;
+  const double* uk[3] = {u0, u1, u2};
+  for (int idx = threadIdx.x; idx < ne * nq; idx += blockDim.x) {
+    const int e = ch.elem_begin + idx / nq, q = idx % nq;
+    double G[NPE][3];
+    ref_grad_f64<NPE>(q, G);
+    double J0[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Gu[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < NPE; i++) {
+      const int l = P.conn_local[(size_t)i * P.E + e];
+      const int lb = ch.local_begin + l;
+      const int g = l < ch.n_own ? ch.own_begin + l : P.local_gid[lb];
+      for (int k = 0; k < 3; k++) {
+        const double X = P.local_x0[(size_t)k * P.Lt + lb], U = uk[k][g];
+        for (int j = 0; j < 3; j++) {
+          J0[3 * k + j] += X * G[i][j];
+          Gu[3 * k + j] += U * G[i][j];
+        }
+      }
+    }
+    const double c00 = J0[4] * J0[8] - J0[5] * J0[7], c01 = J0[5] * J0[6] - J0[3] * J0[8],
+                 c02 = J0[3] * J0[7] - J0[4] * J0[6];
+    const double r = 1.0 / (J0[0] * c00 + J0[1] * c01 + J0[2] * c02);
+    const double Ji[9] = {c00 * r, (J0[2] * J0[7] - J0[1] * J0[8]) * r,
+                          (J0[1] * J0[5] - J0[2] * J0[4]) * r, c01 * r,
+                          (J0[0] * J0[8] - J0[2] * J0[6]) * r, (J0[2] * J0[3] - J0[0] * J0[5]) * r,
+                          c02 * r, (J0[1] * J0[6] - J0[0] * J0[7]) * r,
+                          (J0[0] * J0[4] - J0[1] * J0[3]) * r};
+    double* out = F + 9 * ((size_t)e * nq + q);
+    for (int a = 0; a < 3; a++)
+      for (int j = 0; j < 3; j++)
+        out[3 * a + j] = (a == j ? 1.0 : 0.0) + Gu[3 * a + 0] * Ji[0 * 3 + j] +
+                         Gu[3 * a + 1] * Ji[1 * 3 + j] + Gu[3 * a + 2] * Ji[2 * 3 + j];
+  }
+}
+
 __global__ void k_state_to_caller(const double* u, const double* v, const double* Xc,
                                   const int* node_new, int N, double* xc, double* vc) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -902,6 +963,31 @@ int ci_get_state(ci_solver* s, double* x, double* v, double* mass, float* sigma,
       if (epbar) epbar[o] = hep[qi];
     }
   }
+  return CI_OK;
+}
+
+int ci_deformation_gradient(ci_solver* s, double* F) {
+  if (!s || !F) return fail(CI_ERR_INVALID, "null argument");
+  CI_CUDA(cudaSetDevice(s->device));
+  const int E = s->E, nq = s->nq;
+  const ci::Plan& P = s->plan;
+  DBuf<double> d;
+  CI_CUDA(d.alloc((size_t)9 * E * nq));
+  const ci::DevPlan dp = s->dev_plan();
+  if (s->npe == 4)
+    k_defgrad<4><<<s->C, 128, 0, s->stream>>>(dp, s->d_u.p, s->d_u.p + s->N,
+                                               s->d_u.p + 2 * (size_t)s->N, nq, d.p);
+  else
+    k_defgrad<10><<<s->C, 128, 0, s->stream>>>(dp, s->d_u.p, s->d_u.p + s->N,
+                                                s->d_u.p + 2 * (size_t)s->N, nq, d.p);
+  CI_CUDA(cudaGetLastError());
+  std::vector<double> h((size_t)9 * E * nq);
+  CI_CUDA(cudaMemcpyAsync(h.data(), d.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost,
+                          s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  for (int pe = 0; pe < E; pe++)
+    std::memcpy(F + (size_t)9 * nq * P.elem_orig[pe], h.data() + (size_t)9 * nq * pe,
+                sizeof(double) * 9 * nq);
   return CI_OK;
 }
 

@@ -153,6 +153,12 @@ int ci_get_state(ci_solver* s, double* x, double* v, double* mass, float* sigma,
                  unsigned char* contact);
 /* Overwrite the nodal state (caller order, [3N] each); used for restarts. */
 int ci_set_state(ci_solver* s, const double* x, const double* v);
+/* Deformation gradient F = I + du/dX at every Gauss point of the current state, FP64,
+ * [E*nq*9] in the caller's element order, row-major (F[a][j] = delta_aj + du_a/dX_j).
+ * The reference computes no F (its update works on the displacement increment,
+ * include/dynamics_kernels.h:75-139); this is the reported output of the new
+ * deformation-gradient row. */
+int ci_deformation_gradient(ci_solver* s, double* F);
 /* Binary state file of a started solver -- the state the reference's export_to_vtk
  * dumps (include/dynamics.h:113-254) plus everything a restart needs: positions,
  * velocities, masses, contact history, stored stress and plastic strain at the Gauss

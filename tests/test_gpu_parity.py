@@ -290,3 +290,46 @@ def test_state_file_restart_is_bitwise(cilib, tmp_path, order):
     with pytest.raises(cilib.CiError) as e:
         c.load_state(path)
     assert e.value.code == -1
+
+
+def _ref_grads(order):
+    """Shape-function gradients in reference coordinates at the Gauss points (tet4: one
+    point; tet10: the 4-point rule), the element geometry of include/tetrahedral.h."""
+    dL = np.array([[1.0, 0, 0], [0, 1.0, 0], [-1.0, -1.0, -1.0], [0, 0, 1.0]])
+    if order == 1:
+        return [dL[[2, 0, 1, 3]]]
+    a, b = (5 + 3 * np.sqrt(5)) / 20, (5 - np.sqrt(5)) / 20
+    edges = [(0, 1), (1, 2), (2, 0), (0, 3), (1, 3), (2, 3)]
+    out = []
+    for q in range(4):
+        L = [a if q == 1 else b, a if q == 2 else b, a if q == 0 else b, a if q == 3 else b]
+        G = [(4 * L[c] - 1) * dL[c] for c in range(4)]
+        G += [4 * (L[i] * dL[j] + L[j] * dL[i]) for i, j in edges]
+        out.append(np.array(G))
+    return out
+
+
+@pytest.mark.parametrize("order,n", [(1, 5), (2, 3)])
+def test_deformation_gradient(cilib, order, n):
+    """F = I + du/dX at the Gauss points against an FP64 evaluation from the returned
+    positions (within 1e-5 relative L2 of F - I); rigid start gives F = I."""
+    m = mg.cube(n, order)
+    setup = mg.impact_setup(m, 20.0, 1e-4)
+    s = solver(cilib, m, cilib.MODE_J2, wall_normal=setup["wall_normal"],
+               wall_offset=setup["wall_offset"], wall_stiffness=setup["wall_stiffness"])
+    s.initialize(setup["vel"])
+    F0 = s.deformation_gradient()
+    assert np.abs(F0 - np.eye(3)).max() < 1e-12
+    s.start(setup["dt"])
+    s.step(400)
+    x = s.state(("x",))["x"]
+    F = s.deformation_gradient()
+    X = m.xloc
+    u = x - X
+    Fr = np.zeros_like(F)
+    for q, G in enumerate(_ref_grads(order)):
+        J0 = np.einsum("eia,ij->eaj", X[m.conn], G)
+        Gu = np.einsum("eia,ij->eaj", u[m.conn], G)
+        Fr[:, q] = np.eye(3) + Gu @ np.linalg.inv(J0)
+    assert np.abs(Fr - np.eye(3)).max() > 1e-3, "the case must deform"
+    assert rel(F - np.eye(3), Fr - np.eye(3)) < 1e-5
