@@ -196,6 +196,38 @@ def cpu_baseline(m, setup, seconds_budget: float = 15.0, threads: int | None = N
                       f"(initial + {nsteps} step), RefCompat 5-point K_e, {t:.1f} s"}
 
 
+def fp64_accuracy(m, setup, gpu, nsteps):
+    """Error of the GPU run against the FP64 run of the same formulation (oracle/
+    solver64.cpp, one host thread) on the full mesh after nsteps steps from the same
+    start: relative L2 of the displacement, of the velocity change and of the plastic
+    strain, and whether the contact-node sets agree."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py as op
+    par = op.params(MAT["E"], MAT["nu"], MAT["rho"], MAT["sigma_y0"], MAT["H"], mode=op.J2,
+                    lumping=op.LUMP_HRZ, wall_normal=setup["wall_normal"],
+                    wall_offset=setup["wall_offset"], wall_stiffness=setup["wall_stiffness"])
+    t0 = time.perf_counter()
+    o = op.Solver(m.xloc, m.conn, par)
+    o.initialize(setup["vel"], setup["dt"])
+    o.step(nsteps)
+    ref = o.get()
+    t = time.perf_counter() - t0
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    v0 = np.asarray(setup["vel"], dtype=np.float64)
+    ever, ever_ref = (gpu["contact"] & 2) > 0, (ref["contact"] & 2) > 0
+    return {"vs": "FP64 run of the same formulation (oracle, CPU)", "steps": nsteps,
+            "disp_rel_l2": rel(gpu["x"] - m.xloc, ref["x"] - m.xloc),
+            "dv_rel_l2": rel(gpu["v"] - v0, ref["v"] - v0),
+            "epbar_rel_l2": rel(gpu["epbar"], ref["epbar"]) if ref["epbar"].max() > 0 else None,
+            "epbar_max": float(ref["epbar"].max()),
+            "contact_nodes": int(ever_ref.sum()),
+            "contact_sets_equal": bool(np.array_equal(ever, ever_ref)),
+            "fp64_seconds": round(t, 1)}
+
+
 def run_ours(args, rank, world):
     from cppimpact_gb300 import api
     m, setup, desc = workload(args.workload)
@@ -287,6 +319,20 @@ def run_ours(args, rank, world):
     s.close()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(m, setup, args.cpu_seconds)
+        if args.fp64_check_steps > 0:
+            g = api.Solver(m.xloc, m.conn, **MAT, mode=api.MODE_J2, lumping=api.LUMP_HRZ,
+                           step_kernel=args.step_kernel, chunk_elements=args.chunk_elements,
+                           chunk_nodes=args.chunk_nodes, block_threads=args.block_threads,
+                           elem_lanes=args.elem_lanes, wall_normal=setup["wall_normal"],
+                           wall_offset=setup["wall_offset"],
+                           wall_stiffness=setup["wall_stiffness"],
+                           device=int(os.environ.get("LOCAL_RANK", "0")))
+            g.initialize(setup["vel"])
+            g.start(setup["dt"])
+            g.step(args.fp64_check_steps)
+            line["accuracy"] = fp64_accuracy(m, setup, g.state(("x", "v", "epbar", "contact")),
+                                             args.fp64_check_steps)
+            g.close()
     if rank == 0 and args.sweep:
         line["sweep"] = run_sweep(args)
     return line
@@ -476,6 +522,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-interval", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--fp64-check-steps", type=int, default=20,
+                    help="steps of the GPU-vs-FP64 accuracy check on the full mesh (0: off)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep", type=int, default=1, help="also run the 256-instance batched sweep")
     ap.add_argument("--autotune", type=int, default=128,
