@@ -1,17 +1,21 @@
 // ci_kernels.cuh -- sm_103a kernels of the explicit impact step.
 //
-// K1 k_elem   : one CTA per chunk (see ci_plan.h).  Stages the chunk's nodes in shared
-//               memory (reference coordinates relative to the chunk origin + FP64
-//               displacement rounded to FP32; increment dt v), computes the element
-//               internal force matrix-free in FP32 (FEAnalysis::calculate_f_internal,
-//               include/analysis.h:321-382, without forming B or K_e), updates the J2
-//               state, accumulates node forces in shared memory colour by colour and
-//               writes one partial sum per (chunk, local node) slot.
-// K2 k_node   : one thread per node.  Sums the node's slots in chunk order, a = -f/m,
-//               planar penalty wall and gravity (include/dynamics_kernels.h:150-168,
-//               include/wall.h:37-43), FP64 central-difference update
-//               (include/dynamics.h:477-503).
-// K3 k_elem<MASS_*> + k_mass_sum : lumped mass, once (include/analysis.h:136-162).
+// Fused step (one launch per step, captured in CUDA graphs; one CTA per chunk, see
+// ci_plan.h).  Each CTA (1) completes S^n of every local node of its chunk from S^{n-1}
+// and the previous step's halo (slots summed in fixed order; a = -f/m, planar penalty
+// wall and gravity, include/dynamics_kernels.h:150-168, include/wall.h:37-43; FP64
+// central-difference update, include/dynamics.h:477-503) and stages it in shared
+// memory, (2) computes the element internal force matrix-free in FP32
+// (FEAnalysis::calculate_f_internal, include/analysis.h:321-382, without forming B or
+// K_e) with the J2 update, accumulating node forces in shared memory colour by colour,
+// (3) writes one partial sum per (chunk, local node) slot:
+//   k_step_qp10 : tet10, 4 lanes per element (one per Gauss point), reduce-scatter
+//   k_step_t10  : tet10, one thread per element, barycentric form
+//   k_step      : tet4, one thread per element
+//   k_finalize_nodes : S^N after the last step of a call
+// Two-kernel path and one-shot entry points: k_elem (element work to slots) + k_node
+// (one thread per node); k_elem<MASS_*> + k_mass_sum: lumped mass, once
+// (include/analysis.h:136-162).
 //
 // No float atomics anywhere: every floating-point sum has a fixed order.
 #pragma once
