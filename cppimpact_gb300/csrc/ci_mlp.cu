@@ -1,6 +1,10 @@
 // ci_mlp.cu -- the surrogate's MLP (n_in -> H -> H -> n_out, tanh hidden layers):
 // forward, backward and Adam on the GPU, every matrix product through ci_gemm_bf16
 // (BF16 operands, FP32 accumulation), FP32 master weights, fixed-order reductions.
+// The products of layers 2 and 3 are arranged as A B^T with both operands K-major (the
+// form of the TMA-pipelined tcgen05 kernel): BF16 copies of W2 and W3 are kept
+// transposed, and the weight gradients read transposed activations and output
+// gradients.
 //
 // Parameters, in the order ci_mlp_get_params / set_params use:
 //   W1 [n_in x H], b1 [H], W2 [H x H], b2 [H], W3 [H x n_out], b3 [n_out]
@@ -43,14 +47,16 @@ __global__ void k_to_bf16(const float* in, bf16* out, long long n) {
   if (i < n) out[i] = __float2bfloat16(in[i]);
 }
 
-// dY = scale (Y - T) (scale = 2 / (rows * cols)); per-block partial sum of (Y - T)^2
-__global__ void k_mse_grad(const float* Y, const float* T, float* dY, bf16* dYb, long long n,
-                           float scale, double* part) {
+// dY = scale (Y - T) (scale = 2 / (rows * cols)) for row r = blockIdx.y, whose targets
+// are row idx[r] of T (row r when idx is null); per-block partial sum of (Y - T)^2
+__global__ void k_mse_grad(const float* Y, const float* T, const int* idx, int cols, float* dY,
+                           bf16* dYb, float scale, double* part) {
   __shared__ double red[256];
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int r = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
   double s = 0.0;
-  if (i < n) {
-    const float d = Y[i] - T[i];
+  if (c < cols) {
+    const size_t i = (size_t)r * cols + c;
+    const float d = Y[i] - T[(size_t)(idx ? idx[r] : r) * cols + c];
     dY[i] = scale * d;
     dYb[i] = __float2bfloat16(scale * d);
     s = (double)d * d;
@@ -61,7 +67,7 @@ __global__ void k_mse_grad(const float* Y, const float* T, float* dY, bf16* dYb,
     if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+  if (threadIdx.x == 0) part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
 }
 
 // dZ = dH (1 - H^2)
@@ -74,13 +80,73 @@ __global__ void k_tanh_back(const float* dH, const float* H, float* dZ, bf16* dZ
   }
 }
 
-// column sums of a [rows x cols] matrix, one thread per column, rows in order
-__global__ void k_colsum(const float* A, int rows, int cols, float* out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cols) return;
+// column sums of a [rows x cols] matrix: 32 columns per CTA, 8 row groups (rows
+// r = g, g + 8, ... in order), then the 8 partial sums in group order
+__global__ void __launch_bounds__(256) k_colsum(const float* A, int rows, int cols, float* out) {
+  __shared__ float part[8][33];
+  const int tx = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int c = blockIdx.x * 32 + tx;
   float s = 0.f;
-  for (int r = 0; r < rows; r++) s += A[(size_t)r * cols + c];
-  out[c] = s;
+  if (c < cols)
+    for (int r = g; r < rows; r += 8) s += A[(size_t)r * cols + c];
+  part[g][tx] = s;
+  __syncthreads();
+  if (g == 0 && c < cols) {
+    float t = part[0][tx];
+    for (int k = 1; k < 8; k++) t += part[k][tx];
+    out[c] = t;
+  }
+}
+
+// Layer 1 when n_in is small (the surrogate's 4 impact parameters): Z = tanh(X W1 + b1)
+// with the BF16 operands of the GEMM path, FP32 products summed in input order; writes
+// the FP32 activation and its BF16 copy.
+__global__ void k_layer1_fwd(const bf16* X, const bf16* W1, const float* b1, int rows, int n_in,
+                             int H, float* Z, bf16* Hb) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)rows * H) return;
+  const int r = (int)(i / H), h = (int)(i % H);
+  float acc = 0.f;
+  for (int k = 0; k < n_in; k++)
+    acc = fmaf(__bfloat162float(X[(size_t)r * n_in + k]), __bfloat162float(W1[(size_t)k * H + h]), acc);
+  const float z = tanhf(acc + b1[h]);
+  Z[i] = z;
+  Hb[i] = __float2bfloat16(z);
+}
+
+// gW1 = X^T dZ1 [n_in x H] for small n_in: one thread per entry, rows in order
+__global__ void k_layer1_wgrad(const bf16* X, const bf16* dZb, int rows, int n_in, int H, float* gW) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_in * H) return;
+  const int k = i / H, h = i % H;
+  float acc = 0.f;
+  for (int r = 0; r < rows; r++)
+    acc = fmaf(__bfloat162float(X[(size_t)r * n_in + k]), __bfloat162float(dZb[(size_t)r * H + h]), acc);
+  gW[i] = acc;
+}
+
+// out [cols x rows] (leading dimension ld_out) = in^T, in [rows x cols] (ld_in); 32 x 32
+// tiles through shared memory
+__global__ void __launch_bounds__(256) k_transpose_bf16(const bf16* in, int rows, int cols,
+                                                        int ld_in, bf16* out, int ld_out) {
+  __shared__ bf16 tile[32][34];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int k = ty; k < 32; k += 8) {
+    const int r = r0 + k, c = c0 + tx;
+    if (r < rows && c < cols) tile[k][tx] = in[(size_t)r * ld_in + c];
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int c = c0 + k, r = r0 + tx;
+    if (r < rows && c < cols) out[(size_t)c * ld_out + r] = tile[tx][k];
+  }
+}
+
+inline cudaError_t transpose_bf16(const bf16* in, int rows, int cols, bf16* out, cudaStream_t st) {
+  const dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+  k_transpose_bf16<<<grid, 256, 0, st>>>(in, rows, cols, cols, out, rows);
+  return cudaGetLastError();
 }
 
 // Adam (Kingma & Ba 2015) on FP32 master weights; refreshes the BF16 copy
@@ -99,14 +165,13 @@ __global__ void k_adam(float* p, const float* g, float* m, float* v, bf16* pb, l
   if (pb) pb[i] = __float2bfloat16(pi);
 }
 
-// rows of X picked by idx -> Xb (BF16) and the matching rows of T
-__global__ void k_gather_rows(const float* X, const float* T, const int* idx, int rows, int nx, int nt,
-                              bf16* Xb, float* Tb) {
+// rows of X picked by idx -> Xb (BF16)
+__global__ void k_gather_rows(const float* X, const int* idx, int rows, int nx, bf16* Xb) {
   const int r = blockIdx.x;
   if (r >= rows) return;
   const int s = idx[r];
-  for (int j = threadIdx.x; j < nx; j += blockDim.x) Xb[(size_t)r * nx + j] = __float2bfloat16(X[(size_t)s * nx + j]);
-  for (int j = threadIdx.x; j < nt; j += blockDim.x) Tb[(size_t)r * nt + j] = T[(size_t)s * nt + j];
+  for (int j = threadIdx.x; j < nx; j += blockDim.x)
+    Xb[(size_t)r * nx + j] = __float2bfloat16(X[(size_t)s * nx + j]);
 }
 
 template <typename T>
@@ -134,11 +199,13 @@ struct ci_mlp {
   long long off[6] = {0};     // W1 b1 W2 b2 W3 b3 offsets in the flat arrays
   DBuf<float> p, g, m, v;     // FP32 master params, grads, Adam moments
   DBuf<bf16> pb;              // BF16 copy of the parameters
+  DBuf<bf16> wT;              // BF16 W2^T [H x H] then W3^T [n_out x H]
   DBuf<int> err;
   long long step = 0;
   int cap = 0;                // rows the activation buffers hold
-  DBuf<float> Z1, Z2, Y, T, dY, dH2, dZ2, dH1, dZ1;
+  DBuf<float> Z1, Z2, Y, dY, dH2, dZ2, dH1, dZ1;
   DBuf<bf16> Xb, H1b, H2b, dYb, dZ2b, dZ1b;
+  DBuf<bf16> H1bT, H2bT, dYbT, dZ2bT;  // transposes [cols x rows] for the weight gradients
   DBuf<double> part;
   DBuf<int> idx;
 };
@@ -151,7 +218,6 @@ int ensure_cap(ci_mlp* M, int rows) {
   CM_CUDA(M->Z1.alloc(r * M->H));
   CM_CUDA(M->Z2.alloc(r * M->H));
   CM_CUDA(M->Y.alloc(r * M->n_out));
-  CM_CUDA(M->T.alloc(r * M->n_out));
   CM_CUDA(M->dY.alloc(r * M->n_out));
   CM_CUDA(M->dH2.alloc(r * M->H));
   CM_CUDA(M->dZ2.alloc(r * M->H));
@@ -163,7 +229,11 @@ int ensure_cap(ci_mlp* M, int rows) {
   CM_CUDA(M->dYb.alloc(r * M->n_out));
   CM_CUDA(M->dZ2b.alloc(r * M->H));
   CM_CUDA(M->dZ1b.alloc(r * M->H));
-  CM_CUDA(M->part.alloc(nb(r * M->n_out)));
+  CM_CUDA(M->H1bT.alloc(r * M->H));
+  CM_CUDA(M->H2bT.alloc(r * M->H));
+  CM_CUDA(M->dYbT.alloc(r * M->n_out));
+  CM_CUDA(M->dZ2bT.alloc(r * M->H));
+  CM_CUDA(M->part.alloc(r * nb(M->n_out)));
   CM_CUDA(M->idx.alloc(r));
   M->cap = rows;
   return CI_OK;
@@ -175,29 +245,44 @@ int gemm(ci_mlp* M, const void* A, int lda, int tA, const void* B, int ldb, int 
                       M->err.p, st);
 }
 
+// BF16 W2^T and W3^T from the BF16 parameter copy (after every parameter update)
+int refresh_wT(ci_mlp* M, cudaStream_t st) {
+  CM_CUDA(transpose_bf16(M->pb.p + M->off[2], M->H, M->H, M->wT.p, st));
+  CM_CUDA(transpose_bf16(M->pb.p + M->off[4], M->H, M->n_out, M->wT.p + (size_t)M->H * M->H, st));
+  return CI_OK;
+}
+
 // forward of `rows` rows already in Xb; writes Y (and the hidden activations)
 int forward(ci_mlp* M, int rows, cudaStream_t st) {
   const bf16* W1 = M->pb.p + M->off[0];
-  const bf16* W2 = M->pb.p + M->off[2];
-  const bf16* W3 = M->pb.p + M->off[4];
+  const bf16* W2T = M->wT.p;
+  const bf16* W3T = M->wT.p + (size_t)M->H * M->H;
   const float* b1 = M->p.p + M->off[1];
   const float* b2 = M->p.p + M->off[3];
   const float* b3 = M->p.p + M->off[5];
-  CM_OK(gemm(M, M->Xb.p, M->n_in, 0, W1, M->H, 0, M->Z1.p, M->H, M->H1b.p, rows, M->H, M->n_in, 0.f,
-             b1, 1, st));
-  CM_OK(gemm(M, M->H1b.p, M->H, 0, W2, M->H, 0, M->Z2.p, M->H, M->H2b.p, rows, M->H, M->H, 0.f, b2, 1,
-             st));
-  CM_OK(gemm(M, M->H2b.p, M->H, 0, W3, M->n_out, 0, M->Y.p, M->n_out, nullptr, rows, M->n_out, M->H,
+  if (M->n_in < 16) {
+    k_layer1_fwd<<<nb((long long)rows * M->H), 256, 0, st>>>(M->Xb.p, W1, b1, rows, M->n_in, M->H,
+                                                             M->Z1.p, M->H1b.p);
+    CM_CUDA(cudaGetLastError());
+  } else {
+    CM_OK(gemm(M, M->Xb.p, M->n_in, 0, W1, M->H, 0, M->Z1.p, M->H, M->H1b.p, rows, M->H, M->n_in,
+               0.f, b1, 1, st));
+  }
+  CM_OK(gemm(M, M->H1b.p, M->H, 0, W2T, M->H, 1, M->Z2.p, M->H, M->H2b.p, rows, M->H, M->H, 0.f, b2,
+             1, st));
+  CM_OK(gemm(M, M->H2b.p, M->H, 0, W3T, M->H, 1, M->Y.p, M->n_out, nullptr, rows, M->n_out, M->H,
              0.f, b3, 0, st));
   return CI_OK;
 }
 
-// loss and gradients into M->g for `rows` rows in Xb / T; *loss (may be NULL) gets the
-// mean squared error (host, synchronises)
-int backward(ci_mlp* M, int rows, cudaStream_t st, double* loss) {
+// loss and gradients into M->g for `rows` rows in Xb, whose targets are rows idx[r] of T
+// (rows r when idx is null); *loss (may be NULL) gets the mean squared error (host,
+// synchronises)
+int backward(ci_mlp* M, int rows, cudaStream_t st, double* loss, const float* T, const int* idx) {
   const long long ny = (long long)rows * M->n_out, nh = (long long)rows * M->H;
-  k_mse_grad<<<nb(ny), 256, 0, st>>>(M->Y.p, M->T.p, M->dY.p, M->dYb.p, ny, 2.0f / (float)ny,
-                                     M->part.p);
+  const dim3 mse_grid(nb(M->n_out), rows);
+  k_mse_grad<<<mse_grid, 256, 0, st>>>(M->Y.p, T, idx, M->n_out, M->dY.p, M->dYb.p,
+                                       2.0f / (float)ny, M->part.p);
   float* gW1 = M->g.p + M->off[0];
   float* gb1 = M->g.p + M->off[1];
   float* gW2 = M->g.p + M->off[2];
@@ -206,28 +291,38 @@ int backward(ci_mlp* M, int rows, cudaStream_t st, double* loss) {
   float* gb3 = M->g.p + M->off[5];
   const bf16* W2 = M->pb.p + M->off[2];
   const bf16* W3 = M->pb.p + M->off[4];
-  // layer 3
-  CM_OK(gemm(M, M->H2b.p, M->H, 1, M->dYb.p, M->n_out, 0, gW3, M->n_out, nullptr, M->H, M->n_out,
+  // layer 3: gW3 = H2^T dY as (H2^T) (dY^T)^T
+  CM_CUDA(transpose_bf16(M->H2b.p, rows, M->H, M->H2bT.p, st));
+  CM_CUDA(transpose_bf16(M->dYb.p, rows, M->n_out, M->dYbT.p, st));
+  CM_OK(gemm(M, M->H2bT.p, rows, 0, M->dYbT.p, rows, 1, gW3, M->n_out, nullptr, M->H, M->n_out,
              rows, 0.f, nullptr, 0, st));
-  k_colsum<<<nb(M->n_out), 256, 0, st>>>(M->dY.p, rows, M->n_out, gb3);
+  k_colsum<<<(M->n_out + 31) / 32, 256, 0, st>>>(M->dY.p, rows, M->n_out, gb3);
   CM_OK(gemm(M, M->dYb.p, M->n_out, 0, W3, M->n_out, 1, M->dH2.p, M->H, nullptr, rows, M->H,
              M->n_out, 0.f, nullptr, 0, st));
   // Z2 holds tanh(Z2) = H2 (the GEMM wrote the activated values)
   k_tanh_back<<<nb(nh), 256, 0, st>>>(M->dH2.p, M->Z2.p, M->dZ2.p, M->dZ2b.p, nh);
-  // layer 2
-  CM_OK(gemm(M, M->H1b.p, M->H, 1, M->dZ2b.p, M->H, 0, gW2, M->H, nullptr, M->H, M->H, rows, 0.f,
+  // layer 2: gW2 = H1^T dZ2 as (H1^T) (dZ2^T)^T
+  CM_CUDA(transpose_bf16(M->H1b.p, rows, M->H, M->H1bT.p, st));
+  CM_CUDA(transpose_bf16(M->dZ2b.p, rows, M->H, M->dZ2bT.p, st));
+  CM_OK(gemm(M, M->H1bT.p, rows, 0, M->dZ2bT.p, rows, 1, gW2, M->H, nullptr, M->H, M->H, rows, 0.f,
              nullptr, 0, st));
-  k_colsum<<<nb(M->H), 256, 0, st>>>(M->dZ2.p, rows, M->H, gb2);
+  k_colsum<<<(M->H + 31) / 32, 256, 0, st>>>(M->dZ2.p, rows, M->H, gb2);
   CM_OK(gemm(M, M->dZ2b.p, M->H, 0, W2, M->H, 1, M->dH1.p, M->H, nullptr, rows, M->H, M->H, 0.f,
              nullptr, 0, st));
   k_tanh_back<<<nb(nh), 256, 0, st>>>(M->dH1.p, M->Z1.p, M->dZ1.p, M->dZ1b.p, nh);
   // layer 1
-  CM_OK(gemm(M, M->Xb.p, M->n_in, 1, M->dZ1b.p, M->H, 0, gW1, M->H, nullptr, M->n_in, M->H, rows,
-             0.f, nullptr, 0, st));
-  k_colsum<<<nb(M->H), 256, 0, st>>>(M->dZ1.p, rows, M->H, gb1);
+  if (M->n_in < 16) {
+    k_layer1_wgrad<<<nb((long long)M->n_in * M->H), 256, 0, st>>>(M->Xb.p, M->dZ1b.p, rows, M->n_in,
+                                                                   M->H, gW1);
+    CM_CUDA(cudaGetLastError());
+  } else {
+    CM_OK(gemm(M, M->Xb.p, M->n_in, 1, M->dZ1b.p, M->H, 0, gW1, M->H, nullptr, M->n_in, M->H, rows,
+               0.f, nullptr, 0, st));
+  }
+  k_colsum<<<(M->H + 31) / 32, 256, 0, st>>>(M->dZ1.p, rows, M->H, gb1);
   CM_CUDA(cudaGetLastError());
   if (loss) {
-    std::vector<double> part(nb(ny));
+    std::vector<double> part((size_t)rows * nb(M->n_out));
     CM_CUDA(cudaMemcpyAsync(part.data(), M->part.p, sizeof(double) * part.size(),
                             cudaMemcpyDeviceToHost, st));
     CM_CUDA(cudaStreamSynchronize(st));
@@ -276,7 +371,7 @@ int ci_mlp_create(int n_in, int n_hidden, int n_out, unsigned long long seed, ci
   }
   int rc = CI_OK;
   if (M->p.alloc(o) || M->g.alloc(o) || M->m.alloc(o) || M->v.alloc(o) || M->pb.alloc(o) ||
-      M->err.alloc(1))
+      M->wT.alloc((size_t)n_hidden * n_hidden + (size_t)n_hidden * n_out) || M->err.alloc(1))
     rc = ci::set_last_error(CI_ERR_NOMEM, "ci_mlp_create: device allocation failed");
   if (!rc) rc = ci_mlp_set_params(M, h.data());
   if (!rc && (cudaMemset(M->m.p, 0, sizeof(float) * o) || cudaMemset(M->v.p, 0, sizeof(float) * o) ||
@@ -302,6 +397,7 @@ int ci_mlp_set_params(ci_mlp* M, const float* h) {
   CM_CUDA(cudaMemcpy(M->p.p, h, sizeof(float) * M->np, cudaMemcpyHostToDevice));
   k_to_bf16<<<nb(M->np), 256>>>(M->p.p, M->pb.p, M->np);
   CM_CUDA(cudaGetLastError());
+  CM_OK(refresh_wT(M, 0));
   CM_CUDA(cudaDeviceSynchronize());
   M->step = 0;
   return CI_OK;
@@ -335,9 +431,9 @@ int ci_mlp_gradients(ci_mlp* M, const float* d_X, const float* d_T, int n, float
   std::vector<int> idx(n);
   for (int i = 0; i < n; i++) idx[i] = i;
   CM_CUDA(cudaMemcpy(M->idx.p, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-  k_gather_rows<<<n, 128>>>(d_X, d_T, M->idx.p, n, M->n_in, M->n_out, M->Xb.p, M->T.p);
+  k_gather_rows<<<n, 32>>>(d_X, M->idx.p, n, M->n_in, M->Xb.p);
   CM_OK(forward(M, n, 0));
-  CM_OK(backward(M, n, 0, loss));
+  CM_OK(backward(M, n, 0, loss, d_T, nullptr));
   if (h_grad) CM_CUDA(cudaMemcpy(h_grad, M->g.p, sizeof(float) * M->np, cudaMemcpyDeviceToHost));
   return check_err(M, 0);
 }
@@ -359,12 +455,11 @@ int ci_mlp_train(ci_mlp* M, const float* d_X, const float* d_T, int n, int batch
     double ep_loss = 0.0;
     int nbatches = 0;
     for (int b0 = 0; b0 + batch <= n; b0 += batch) {
-      k_gather_rows<<<batch, 128, 0, st>>>(d_X, d_T, M->idx.p + b0, batch, M->n_in, M->n_out,
-                                           M->Xb.p, M->T.p);
+      k_gather_rows<<<batch, 32, 0, st>>>(d_X, M->idx.p + b0, batch, M->n_in, M->Xb.p);
       CM_OK(forward(M, batch, st));
       const bool last = b0 + 2 * batch > n;
       double l = 0.0;
-      CM_OK(backward(M, batch, st, (h_loss && last) ? &l : nullptr));
+      CM_OK(backward(M, batch, st, (h_loss && last) ? &l : nullptr, d_T, M->idx.p + b0));
       ep_loss += l;
       nbatches += last ? 1 : 0;
       M->step++;
@@ -372,6 +467,7 @@ int ci_mlp_train(ci_mlp* M, const float* d_X, const float* d_T, int n, int batch
       k_adam<<<nb(M->np), 256, 0, st>>>(M->p.p, M->g.p, M->m.p, M->v.p, M->pb.p, M->np, lr, b1, b2,
                                         eps, c1, c2);
       CM_CUDA(cudaGetLastError());
+      CM_OK(refresh_wT(M, st));
     }
     if (h_loss) h_loss[ep] = nbatches ? ep_loss / nbatches : 0.0;
   }
