@@ -114,15 +114,19 @@ __global__ void k_layer1_fwd(const bf16* X, const bf16* W1, const float* b1, int
   Hb[i] = __float2bfloat16(z);
 }
 
-// gW1 = X^T dZ1 [n_in x H] for small n_in: one thread per entry, rows in order
+// gW1 = X^T dZ1 [n_in x H] for small n_in: one warp per entry; lane j sums rows j, j+32,
+// ... in order, then the 32 lane sums in a fixed butterfly order
 __global__ void k_layer1_wgrad(const bf16* X, const bf16* dZb, int rows, int n_in, int H, float* gW) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_in * H) return;
-  const int k = i / H, h = i % H;
+  const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= n_in * H) return;
+  const int k = w / H, h = w % H;
   float acc = 0.f;
-  for (int r = 0; r < rows; r++)
+  for (int r = lane; r < rows; r += 32)
     acc = fmaf(__bfloat162float(X[(size_t)r * n_in + k]), __bfloat162float(dZb[(size_t)r * H + h]), acc);
-  gW[i] = acc;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) gW[w] = acc;
 }
 
 // out [cols x rows] (leading dimension ld_out) = in^T, in [rows x cols] (ld_in); 32 x 32
@@ -312,8 +316,8 @@ int backward(ci_mlp* M, int rows, cudaStream_t st, double* loss, const float* T,
   k_tanh_back<<<nb(nh), 256, 0, st>>>(M->dH1.p, M->Z1.p, M->dZ1.p, M->dZ1b.p, nh);
   // layer 1
   if (M->n_in < 16) {
-    k_layer1_wgrad<<<nb((long long)M->n_in * M->H), 256, 0, st>>>(M->Xb.p, M->dZ1b.p, rows, M->n_in,
-                                                                   M->H, gW1);
+    k_layer1_wgrad<<<nb(32LL * M->n_in * M->H), 256, 0, st>>>(M->Xb.p, M->dZ1b.p, rows, M->n_in,
+                                                               M->H, gW1);
     CM_CUDA(cudaGetLastError());
   } else {
     CM_OK(gemm(M, M->Xb.p, M->n_in, 1, M->dZ1b.p, M->H, 0, gW1, M->H, nullptr, M->n_in, M->H, rows,
