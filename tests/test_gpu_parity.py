@@ -161,15 +161,19 @@ def test_refcompat_trajectory_vs_reference_tet4(cilib):
     assert rel(st["x"] - g["xloc"], g["x"] - g["xloc"]) < 1e-3
 
 
-@pytest.mark.parametrize("order,n,steps,speed,chunks", [(1, 6, 800, 30.0, (0, 0)),
-                                                      (2, 3, 600, 20.0, (0, 0)),
-                                                      (2, 4, 600, 20.0, (4096, 896)),
-                                                      (1, 8, 600, 30.0, (4096, 896))])
-def test_j2_trajectory_vs_fp64(cilib, oracle, order, n, steps, speed, chunks):
+@pytest.mark.parametrize("order,n,steps,speed,chunks,lanes", [(1, 6, 800, 30.0, (0, 0), 0),
+                                                            (2, 3, 600, 20.0, (0, 0), 4),
+                                                            (2, 3, 600, 20.0, (0, 0), 1),
+                                                            (2, 4, 600, 20.0, (4096, 896), 4),
+                                                            (2, 4, 600, 20.0, (4096, 896), 1),
+                                                            (1, 8, 600, 30.0, (4096, 896), 0)])
+def test_j2_trajectory_vs_fp64(cilib, oracle, order, n, steps, speed, chunks, lanes):
+    """tet10 with 4 lanes per element (k_step_qp10) and one thread per element
+    (k_step_t10, barycentric form)."""
     m = mg.cube(n, order)
     setup = mg.impact_setup(m, speed, 1e-4)
     s = _run_gpu(cilib, m, setup, cilib.MODE_J2, steps, chunk_elements=chunks[0],
-                 chunk_nodes=chunks[1])
+                 chunk_nodes=chunks[1], elem_lanes=lanes)
     st = s.state()
     ref = _run_oracle(oracle, m, setup, oracle.J2, steps, oracle.LUMP_HRZ)
     assert ref["epbar"].max() > 0, "the case must yield"
