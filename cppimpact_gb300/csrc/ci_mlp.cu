@@ -48,7 +48,9 @@ __global__ void k_to_bf16(const float* in, bf16* out, long long n) {
 }
 
 // dY = scale (Y - T) (scale = 2 / (rows * cols)) for row r = blockIdx.y, whose targets
-// are row idx[r] of T (row r when idx is null); per-block partial sum of (Y - T)^2
+// are row idx[r] of T (row r when idx is null); with LOSS, per-block partial sums of
+// (Y - T)^2
+template <bool LOSS>
 __global__ void k_mse_grad(const float* Y, const float* T, const int* idx, int cols, float* dY,
                            bf16* dYb, float scale, double* part) {
   __shared__ double red[256];
@@ -61,6 +63,7 @@ __global__ void k_mse_grad(const float* Y, const float* T, const int* idx, int c
     dYb[i] = __float2bfloat16(scale * d);
     s = (double)d * d;
   }
+  if (!LOSS) return;
   red[threadIdx.x] = s;
   __syncthreads();
   for (int o = 128; o > 0; o >>= 1) {
@@ -285,8 +288,12 @@ int forward(ci_mlp* M, int rows, cudaStream_t st) {
 int backward(ci_mlp* M, int rows, cudaStream_t st, double* loss, const float* T, const int* idx) {
   const long long ny = (long long)rows * M->n_out, nh = (long long)rows * M->H;
   const dim3 mse_grid(nb(M->n_out), rows);
-  k_mse_grad<<<mse_grid, 256, 0, st>>>(M->Y.p, T, idx, M->n_out, M->dY.p, M->dYb.p,
-                                       2.0f / (float)ny, M->part.p);
+  if (loss)
+    k_mse_grad<true><<<mse_grid, 256, 0, st>>>(M->Y.p, T, idx, M->n_out, M->dY.p, M->dYb.p,
+                                               2.0f / (float)ny, M->part.p);
+  else
+    k_mse_grad<false><<<mse_grid, 256, 0, st>>>(M->Y.p, T, idx, M->n_out, M->dY.p, M->dYb.p,
+                                                2.0f / (float)ny, M->part.p);
   float* gW1 = M->g.p + M->off[0];
   float* gb1 = M->g.p + M->off[1];
   float* gW2 = M->g.p + M->off[2];

@@ -538,3 +538,34 @@ def study(cfg: Config, plain_sample: int = 4, audit_fail_fraction: float = 0.1) 
     out["speedup_vs_plain_gpu"] = out["runs_per_hour"]["surrogate"] / out["runs_per_hour"]["plain_gpu_solver"]
     out["gemm"] = gemm_tflops(cfg.n_train * cfg.snaps, 3 * mesh.num_nodes, cfg.rank + 32)
     return out
+
+
+def time_training(n_in=4, hidden=256, n_out=5120, rows=4096, batch=256, epochs=20, seed=0):
+    """Milliseconds per training epoch of one MLP member (ci_mlp_train) on seeded random
+    data of the surrogate's shapes."""
+    torch = _torch()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    X = torch.randn(rows, n_in, device="cuda", generator=g)
+    T = 0.1 * torch.randn(rows, n_out, device="cuda", generator=g)
+    net = MLP(n_in, hidden, n_out, seed + 1)
+    net.train(X, T, 1, batch, 2e-3, seed)  # warm-up (tensor maps, first launches)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net.train(X, T, epochs, batch, 2e-3, seed)
+    torch.cuda.synchronize()
+    ms = 1e3 * (time.perf_counter() - t0) / epochs
+    net.close()
+    return ms
+
+
+if __name__ == "__main__":
+    import argparse
+
+    ap = argparse.ArgumentParser(description="time one surrogate MLP member's training")
+    ap.add_argument("--hidden", type=int, default=256)
+    ap.add_argument("--n-out", type=int, default=5120)
+    ap.add_argument("--epochs", type=int, default=20)
+    a = ap.parse_args()
+    print(f"{a.epochs} epochs, 4 -> {a.hidden} -> {a.hidden} -> {a.n_out}: "
+          f"{time_training(hidden=a.hidden, n_out=a.n_out, epochs=a.epochs):.2f} ms/epoch")
