@@ -240,16 +240,16 @@ def test_nonfinite_state_reported(cilib):
     assert ei.value.code == -4
 
 
-@pytest.mark.parametrize("order", [1, 2])
-def test_fused_step_split_invariance(cilib, order):
+@pytest.mark.parametrize("order,lanes", [(1, 0), (2, 4), (2, 1)])
+def test_fused_step_split_invariance(cilib, order, lanes):
     """The fused path finalises boundary nodes either at the start of the next step or
     in the end-of-call kernel; both use the same rounding, so splitting a run into
     calls of any length (graph-captured or not, odd or even) changes no bit."""
     m = mg.cube(5, order)
     setup = mg.impact_setup(m, 20.0, 1e-4)
-    a = _run_gpu(cilib, m, setup, cilib.MODE_J2, 0, graph_steps=8)
+    a = _run_gpu(cilib, m, setup, cilib.MODE_J2, 0, graph_steps=8, elem_lanes=lanes)
     a.step(77)
-    b = _run_gpu(cilib, m, setup, cilib.MODE_J2, 0, graph_steps=8)
+    b = _run_gpu(cilib, m, setup, cilib.MODE_J2, 0, graph_steps=8, elem_lanes=lanes)
     for n in (1, 2, 9, 16, 17, 32):
         b.step(n)
     sa, sb = a.state(), b.state()
@@ -257,11 +257,11 @@ def test_fused_step_split_invariance(cilib, order):
         assert np.array_equal(sa[k], sb[k]), k
 
 
-@pytest.mark.parametrize("order", [1, 2])
-def test_fused_matches_two_kernel_path(cilib, order):
+@pytest.mark.parametrize("order,lanes", [(1, 0), (2, 4), (2, 1)])
+def test_fused_matches_two_kernel_path(cilib, order, lanes):
     m = mg.cube(5, order)
     setup = mg.impact_setup(m, 20.0, 1e-4)
-    a = _run_gpu(cilib, m, setup, cilib.MODE_J2, 300).state()
+    a = _run_gpu(cilib, m, setup, cilib.MODE_J2, 300, elem_lanes=lanes).state()
     b = _run_gpu(cilib, m, setup, cilib.MODE_J2, 300, step_kernel=1).state()
     assert rel(a["x"] - m.xloc, b["x"] - m.xloc) < 1e-5
     assert rel(a["epbar"], b["epbar"]) < 1e-4
