@@ -48,7 +48,7 @@ class Config:
     batch: int = 256
     lr: float = 2e-3
     ensemble: int = 5
-    spread_threshold: float = 0.01
+    spread_threshold: float = 0.0075
     audit_fraction: float = 0.05
     error_threshold: float = 0.02
     seed: int = mg.DEFAULT_SEED
@@ -519,7 +519,7 @@ def study(cfg: Config, plain_sample: int = 4, audit_fail_fraction: float = 0.1) 
         {"threshold": th, "flagged": int((spread > th).sum()),
          "unflagged_frac_over_2pct": float((err_only[spread <= th] > 0.02).mean()) if (spread <= th).any() else 0.0,
          "unflagged_max": float(err_only[spread <= th].max()) if (spread <= th).any() else 0.0}
-        for th in (0.0025, 0.005, 0.01, 0.02)]
+        for th in (0.0025, 0.005, 0.0075, 0.01, 0.02)]
     plain = plain_run_ms(pte[:plain_sample], cfg, mesh)
     plain_ms = float(np.mean(plain))
     out["timing"] = {"predict_s": t_pred, "fallback_wall_s": t_fb, "fallback_device_ms": fb_ms,
