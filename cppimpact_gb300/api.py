@@ -112,6 +112,7 @@ EXPORTS = {
     "ci_batch_destroy": (C.c_int, [C.c_void_p]),
     "ci_batch_tuning": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, _fp]),
     "ci_batch_run_snapshots": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, _fp]),
+    "ci_batch_run_peaks": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _fp, _fp, _fp]),
     "ci_batch_node_order": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip]),
     "ci_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
     "ci_mlp_destroy": (C.c_int, [C.c_void_p]),
@@ -403,6 +404,17 @@ class Batch:
         check(lib().ci_batch_run_snapshots(self._h, int(every), C.c_void_p(d_snap_ptr),
                                            int(max_snaps), C.byref(ms)))
         return ms.value
+
+    def run_peaks(self, every, max_snaps):
+        """Run keeping per instance the largest displacement norm over the snapshot
+        states and the final largest equivalent plastic strain (ci_batch_run_peaks):
+        (peak_disp [n], peak_epbar [n], device ms)."""
+        n = len(self._meshes)
+        pd, pe = np.zeros(n, dtype=np.float32), np.zeros(n, dtype=np.float32)
+        ms = C.c_float(0)
+        check(lib().ci_batch_run_peaks(self._h, int(every), int(max_snaps), _f(pd), _f(pe),
+                                       C.byref(ms)))
+        return pd, pe, ms.value
 
     def node_order(self, i):
         m = self._meshes[i]

@@ -599,17 +599,18 @@ int autotune_group(ci_batch* b, Group& G, const ci_instance* in, const ci_option
 // snap[(k / every - 1)][node][3] (plan order).  A node of an instance still stepping
 // is completed from S^{k-1} and the halo of step k-1 exactly as step k will do it;
 // instances that have finished (k > nsteps) hold their final state in buffer nsteps & 1.
-__global__ void k_snapshot(FusedArgs A0, FusedArgs A1, const int* node_inst, int N, int every,
-                           float* snap, int max_snaps) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
+// Displacement of node n at the snapshot the current tick ends (the state after
+// k = *step_ctr steps of its instance, or its final state once it has stopped); false
+// outside the snapshot range.
+__device__ __forceinline__ bool snapshot_u(const FusedArgs& A0, const FusedArgs& A1,
+                                           const int* node_inst, int n, int every, int max_snaps,
+                                           double (&u)[3], int& si, int& inst) {
   const int k = *A0.step_ctr;
-  const int si = k / every - 1;
-  if (si < 0 || si >= max_snaps) return;
-  const int inst = node_inst[n];
+  si = k / every - 1;
+  if (si < 0 || si >= max_snaps) return false;
+  inst = node_inst[n];
   const int ns = A0.inst_nsteps[inst];
   // A0: views with cur = buffer A (even k), A1: cur = buffer B
-  double u[3];
   if (k > ns) {
     const FusedArgs& F = (ns & 1) ? A1 : A0;
     for (int c = 0; c < 3; c++) u[c] = F.u_cur[c][n];
@@ -622,10 +623,48 @@ __global__ void k_snapshot(FusedArgs A0, FusedArgs A1, const int* node_inst, int
     complete_node(F, F.inst_np[inst], n, F.P.slot_row[n], F.P.slot_row[n + 1], u, v, a, hit, uf,
                   vf);
   }
+  return true;
+}
+
+__global__ void k_snapshot(FusedArgs A0, FusedArgs A1, const int* node_inst, int N, int every,
+                           float* snap, int max_snaps) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double u[3];
+  int si, inst;
+  if (!snapshot_u(A0, A1, node_inst, n, every, max_snaps, u, si, inst)) return;
   float* o = snap + ((size_t)si * N + n) * 3;
   o[0] = (float)u[0];
   o[1] = (float)u[1];
   o[2] = (float)u[2];
+}
+
+// Running maximum per instance of the nodal displacement norm at the snapshot times,
+// from the FP32 displacement the snapshots hold; non-negative floats order like their
+// bit patterns, so the integer maximum is exact and independent of the order.
+__global__ void k_snapshot_peak(FusedArgs A0, FusedArgs A1, const int* node_inst, int N, int every,
+                                int max_snaps, float* inst_peak) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double u[3];
+  int si, inst;
+  if (!snapshot_u(A0, A1, node_inst, n, every, max_snaps, u, si, inst)) return;
+  const float x = (float)u[0], y = (float)u[1], z = (float)u[2];
+  const float m = sqrtf(x * x + y * y + z * z);
+  atomicMax(reinterpret_cast<int*>(inst_peak) + inst, __float_as_int(m));
+}
+
+// Largest equivalent plastic strain per instance (one CTA per chunk, integer maximum of
+// the non-negative float bits).
+__global__ void k_peak_epbar(const ChunkInfo* chunks, const float* epbar, int nq, float* inst_peak) {
+  const ChunkInfo ch = chunks[blockIdx.x];
+  float m = 0.f;
+  for (long long i = (long long)ch.elem_begin * nq + threadIdx.x; i < (long long)ch.elem_end * nq;
+       i += blockDim.x)
+    m = fmaxf(m, epbar[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int*>(inst_peak) + ch.inst, __float_as_int(m));
 }
 
 }  // namespace
@@ -785,14 +824,19 @@ int ci_batch_get_state(ci_batch* b, int i, double* x, double* v, float* epbar,
   return CI_OK;
 }
 
-int ci_batch_run_snapshots(ci_batch* b, int every, float* d_snap, int max_snaps, float* device_ms) {
-  if (!b || every <= 0 || (every & 1) || !d_snap || max_snaps <= 0)
-    return fail(CI_ERR_INVALID, "ci_batch_run_snapshots: needs an even interval and a buffer");
+}  // extern "C"
+
+namespace {
+
+// Runs every instance in graphs of `every` steps, each followed by the step tick and
+// tail(G) (kernels on G.stream, captured into the graph); the device time goes to
+// *device_ms.  One element type per batch.
+template <class Tail>
+int run_intervals(ci_batch* b, int every, float* device_ms, const char* what, Tail tail) {
   if (b->g[0] && b->g[1])
-    return fail(CI_ERR_UNSUPPORTED, "ci_batch_run_snapshots: one element type per batch");
+    return fail(CI_ERR_UNSUPPORTED, std::string(what) + ": one element type per batch");
   CB_CUDA(cudaSetDevice(b->device));
   Group& G = *(b->g[0] ? b->g[0] : b->g[1]);
-  // graph: `every` steps, then the snapshot of the state after them, then the tick
   if (G.graph) cudaGraphExecDestroy(G.graph);
   G.graph = nullptr;
   cudaGraph_t g = nullptr;
@@ -804,23 +848,20 @@ int ci_batch_run_snapshots(ci_batch* b, int every, float* d_snap, int max_snaps,
   }
   if (err == cudaSuccess) {
     k_tick<<<1, 1, 0, G.stream>>>(G.step_ctr.p, every);
-    k_snapshot<<<(G.N + 255) / 256, 256, 0, G.stream>>>(group_args(G, 0), group_args(G, 1),
-                                                        G.node_inst.p, G.N, every, d_snap, max_snaps);
+    tail(G);
     err = cudaGetLastError();
   }
   cudaError_t e2 = cudaStreamEndCapture(G.stream, &g);
   if (err != cudaSuccess || e2 != cudaSuccess)
-    return fail(CI_ERR_CUDA, std::string("snapshot capture: ") +
+    return fail(CI_ERR_CUDA, std::string(what) + " capture: " +
                                  cudaGetErrorString(err != cudaSuccess ? err : e2));
   err = cudaGraphInstantiate(&G.graph, g, 0);
   cudaGraphDestroy(g);
-  if (err != cudaSuccess) return fail(CI_ERR_CUDA, std::string("snapshot graph: ") + cudaGetErrorString(err));
+  if (err != cudaSuccess) return fail(CI_ERR_CUDA, std::string(what) + " graph: " + cudaGetErrorString(err));
   CB_CUDA(cudaEventRecord(b->ev0, G.stream));
-  // enqueue_run launches ceil((max_steps + 1) / every) graphs of `every` steps
+  // ceil((max_steps + 1) / every) graphs of `every` steps, prepared like a normal run
   {
-    const int total = G.max_steps + 1;
-    // same preparation as a normal run, with the snapshot graph
-    const int rc = enqueue_run_graph(G, total, every);
+    const int rc = enqueue_run_graph(G, G.max_steps + 1, every);
     if (rc) return rc;
   }
   CB_CUDA(cudaEventRecord(b->ev1, G.stream));
@@ -834,6 +875,47 @@ int ci_batch_run_snapshots(ci_batch* b, int every, float* d_snap, int max_snaps,
   CB_CUDA(cudaMemcpy(&stw, G.status.p, sizeof(stw), cudaMemcpyDeviceToHost));
   if (stw & ST_NONFINITE) return fail(CI_ERR_NONFINITE, "non-finite nodal state");
   b->done = true;
+  return CI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ci_batch_run_snapshots(ci_batch* b, int every, float* d_snap, int max_snaps, float* device_ms) {
+  if (!b || every <= 0 || (every & 1) || !d_snap || max_snaps <= 0)
+    return fail(CI_ERR_INVALID, "ci_batch_run_snapshots: needs an even interval and a buffer");
+  return run_intervals(b, every, device_ms, "ci_batch_run_snapshots", [&](Group& G) {
+    k_snapshot<<<(G.N + 255) / 256, 256, 0, G.stream>>>(group_args(G, 0), group_args(G, 1),
+                                                        G.node_inst.p, G.N, every, d_snap, max_snaps);
+  });
+}
+
+int ci_batch_run_peaks(ci_batch* b, int every, int max_snaps, float* peak_disp, float* peak_epbar,
+                       float* device_ms) {
+  if (!b || every <= 0 || (every & 1) || max_snaps <= 0)
+    return fail(CI_ERR_INVALID, "ci_batch_run_peaks: needs an even interval");
+  int rc = run_intervals(b, every, device_ms, "ci_batch_run_peaks", [&](Group& G) {
+    k_snapshot_peak<<<(G.N + 255) / 256, 256, 0, G.stream>>>(group_args(G, 0), group_args(G, 1),
+                                                             G.node_inst.p, G.N, every, max_snaps,
+                                                             G.peak.p);
+  });
+  if (rc) return rc;
+  Group& G = *(b->g[0] ? b->g[0] : b->g[1]);
+  const size_t ni = G.insts.size();
+  DBuf<float> d_ep;
+  CB_CUDA(d_ep.alloc(ni));
+  CB_CUDA(cudaMemsetAsync(d_ep.p, 0, sizeof(float) * ni, G.stream));
+  k_peak_epbar<<<G.C, 256, 0, G.stream>>>(G.chunks.p, G.epbar.p, G.nq, d_ep.p);
+  CB_CUDA(cudaGetLastError());
+  std::vector<float> hd(ni), he(ni);
+  CB_CUDA(cudaMemcpyAsync(hd.data(), G.peak.p, sizeof(float) * ni, cudaMemcpyDeviceToHost, G.stream));
+  CB_CUDA(cudaMemcpyAsync(he.data(), d_ep.p, sizeof(float) * ni, cudaMemcpyDeviceToHost, G.stream));
+  CB_CUDA(cudaStreamSynchronize(G.stream));
+  for (size_t k = 0; k < ni; k++) {
+    if (peak_disp) peak_disp[G.insts[k]] = hd[k];
+    if (peak_epbar) peak_epbar[G.insts[k]] = he[k];
+  }
   return CI_OK;
 }
 

@@ -124,9 +124,11 @@ def jacobi_eigh(A: np.ndarray, sweeps: int = 60, tol: float = 1e-14):
 
 
 def _instances(params, cfg, mesh):
+    # the wall stiffness and the stable dt depend on the mesh only
+    k, dt = mg.wall_stiffness(mesh, E), mg.cfl_dt(mesh, E, NU, RHO)
     inst = []
     for v, sy, h, tilt in params:
-        st = tilted_setup(mesh, v, tilt)
+        st = tilted_setup(mesh, v, tilt, stiffness=k, dt=dt)
         st["t_end"] = (cfg.steps - 0.5) * st["dt"]
         inst.append(dict(xloc=mesh.xloc, conn=mesh.conn, E=E, nu=NU, rho=RHO, sigma_y0=sy,
                          H=h * E, **st))
@@ -373,8 +375,11 @@ def fallback_runs(params: np.ndarray, cfg: Config, mesh=None, shape=None):
     plastic strain, device ms."""
     if len(params) == 0:
         return np.zeros(0), np.zeros(0), 0.0
-    s, ep, ms = generate(params, cfg, mesh, shape)
-    return peak_disp(s).cpu().numpy(), ep, ms
+    mesh = mesh or mg.cube(cfg.n_cube, 1)
+    b = api.Batch(_instances(params, cfg, mesh), **(shape or {}))
+    pd, pe, ms = b.run_peaks(cfg.every, cfg.snaps)
+    b.close()
+    return pd.astype(np.float64), pe.astype(np.float64), ms
 
 
 def plain_run_ms(params: np.ndarray, cfg: Config, mesh=None) -> list[float]:

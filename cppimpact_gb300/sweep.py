@@ -16,13 +16,17 @@ from . import meshgen as mg
 E, NU, RHO = 68.9e9, 0.33, 2700.0
 
 
-def tilted_setup(mesh: mg.TetMesh, speed: float, tilt_deg: float, gap: float = 1e-3) -> dict:
+def tilted_setup(mesh: mg.TetMesh, speed: float, tilt_deg: float, gap: float = 1e-3,
+                 stiffness: float | None = None, dt: float | None = None) -> dict:
+    """Wall tilted by tilt_deg about x, `gap` below the mesh, impact speed along -z;
+    stiffness and dt (mesh properties) may be passed in when many instances share a mesh."""
     th = math.radians(tilt_deg)
     n = np.array([0.0, math.sin(th), math.cos(th)])
     d = mesh.xloc @ n
     return dict(wall_normal=tuple(n), wall_offset=float(d.min() - gap),
-                wall_stiffness=mg.wall_stiffness(mesh, E), vel=(0.0, 0.0, -float(speed)),
-                dt=mg.cfl_dt(mesh, E, NU, RHO))
+                wall_stiffness=mg.wall_stiffness(mesh, E) if stiffness is None else stiffness,
+                vel=(0.0, 0.0, -float(speed)),
+                dt=mg.cfl_dt(mesh, E, NU, RHO) if dt is None else dt)
 
 
 def make_instances(count: int = 256, seed: int = mg.DEFAULT_SEED, t_end: float = 2e-3,

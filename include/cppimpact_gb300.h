@@ -226,6 +226,14 @@ int ci_batch_tuning(ci_batch* b, int npe, int* chunk_elements, int* chunk_nodes,
  * and its offset in N_total. */
 int ci_batch_run_snapshots(ci_batch* b, int every, float* d_snap, int max_snaps, float* device_ms);
 int ci_batch_node_order(ci_batch* b, int i, int* perm, int* node_offset);
+/* Runs the batch like ci_batch_run_snapshots but keeps only, per instance, the largest
+ * nodal displacement norm over the same max_snaps snapshot states (FP32, like the
+ * snapshots) and the largest equivalent plastic strain of the final state:
+ * peak_disp [n], peak_epbar [n] (either may be NULL), in instance order.  The
+ * reference has no counterpart (its drivers write VTK files, include/dynamics.h:113-254);
+ * this is the sweep's per-run answer without the snapshot buffer. */
+int ci_batch_run_peaks(ci_batch* b, int every, int max_snaps, float* peak_disp, float* peak_epbar,
+                       float* device_ms);
 
 /* ---- BF16 tensor-core GEMM (surrogate training and inference; no reference
  * counterpart: the reference has no dense contraction) ----

@@ -95,6 +95,22 @@ def test_snapshots_match_final_state(cilib):
         assert np.abs(got - u).max() <= 2e-7 * np.abs(u).max() + 1e-15
 
 
+def test_run_peaks_match_snapshots(cilib):
+    """ci_batch_run_peaks keeps per run the largest displacement norm over the snapshot
+    states (the same FP32 values the snapshots hold) and the final largest plastic
+    strain: equal to the snapshot path up to the FP32 norm's rounding, and exactly."""
+    pytest.importorskip("torch")
+    from cppimpact_gb300 import surrogate as sg
+    cfg = sg.Config(n_cube=4, steps=400, every=50)
+    params = sg.sample_params(6, np.random.default_rng(11))
+    snaps, peak_ep, _ = sg.generate(params, cfg)
+    ref = sg.peak_disp(snaps).cpu().numpy().astype(np.float64)
+    pd, pe, ms = sg.fallback_runs(params, cfg)
+    assert ms > 0 and ref.min() > 0
+    assert np.abs(pd - ref).max() <= 1e-6 * ref.max()
+    assert np.array_equal(pe.astype(np.float32), peak_ep.astype(np.float32))
+
+
 def test_small_surrogate_end_to_end(cilib):
     pytest.importorskip("torch")
     from cppimpact_gb300 import surrogate as sg
