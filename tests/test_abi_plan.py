@@ -137,3 +137,20 @@ def test_inp_reader_on_reference_inputs(cilib, name, npe):
     assert np.array_equal(mesh.element_nodes, py.conn)
     assert np.array_equal(mesh.slave_nodes, py.slave)
     cilib.plan_verify(py.xloc, py.conn)
+
+
+def test_surrogate_instances_share_mesh_properties():
+    """Instances of one mesh get the wall stiffness and dt computed once; the values are
+    those of the per-instance setup."""
+    from cppimpact_gb300 import meshgen as mg
+    from cppimpact_gb300 import surrogate as sg
+    from cppimpact_gb300.sweep import tilted_setup
+    cfg = sg.Config(n_cube=3, steps=200, every=50)
+    m = mg.cube(3, 1)
+    params = sg.sample_params(4, np.random.default_rng(5))
+    inst = sg._instances(params, cfg, m)
+    for d, (v, sy, h, tilt) in zip(inst, params):
+        ref = tilted_setup(m, v, tilt)
+        for k in ("wall_normal", "wall_offset", "wall_stiffness", "vel", "dt"):
+            assert d[k] == ref[k], k
+        assert d["t_end"] == (cfg.steps - 0.5) * ref["dt"]
