@@ -473,6 +473,31 @@ cudaError_t launch_tma(const CUtensorMap& ta, const CUtensorMap& tb, dim3 grid, 
   return cudaGetLastError();
 }
 
+// Tiny products (the plastic-strain network's 64-wide layers) on the CUDA cores: one
+// thread per output, the BF16 operands' products summed in FP32 in K order, then the
+// epilogue of the tensor-core kernels (alpha, beta, bias, tanh, BF16 copy).
+__global__ void __launch_bounds__(256) k_gemm_small(const __nv_bfloat16* A, int lda, int tA,
+                                                    const __nv_bfloat16* B, int ldb, int tB,
+                                                    float* C, int ldc, __nv_bfloat16* Cb, int M,
+                                                    int N, int K, float alpha, float beta,
+                                                    const float* bias, int act) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)M * N) return;
+  const int row = (int)(i / N), col = (int)(i % N);
+  float acc = 0.f;
+  for (int k = 0; k < K; k++) {
+    const float a = __bfloat162float(tA ? A[(size_t)k * lda + row] : A[(size_t)row * lda + k]);
+    const float b = __bfloat162float(tB ? B[(size_t)col * ldb + k] : B[(size_t)k * ldb + col]);
+    acc = fmaf(a, b, acc);
+  }
+  float v = alpha * acc;
+  if (beta != 0.f) v += beta * C[(size_t)row * ldc + col];
+  if (bias) v += bias[col];
+  if (act == 1) v = tanhf(v);
+  C[(size_t)row * ldc + col] = v;
+  if (Cb) Cb[(size_t)row * ldc + col] = __float2bfloat16(v);
+}
+
 }  // namespace
 
 extern "C" int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, int ldb, int transB,
@@ -485,9 +510,23 @@ extern "C" int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, i
     return ci::set_last_error(CI_ERR_INVALID, "ci_gemm_bf16: activation must be 0 or 1");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // A B^T with both operands K-major and TMA-compatible rows: the pipelined kernel
-  bool tma = !transA && transB && M >= BM && N >= 16 && K >= TBK && lda >= K && ldb >= K &&
-             lda % 8 == 0 && ldb % 8 == 0 && reinterpret_cast<uintptr_t>(A) % 16 == 0 &&
-             reinterpret_cast<uintptr_t>(B) % 16 == 0;
+  const bool tma_shape = !transA && transB && M >= BM && N >= 16 && K >= TBK && lda >= K &&
+                         ldb >= K && lda % 8 == 0 && ldb % 8 == 0 &&
+                         reinterpret_cast<uintptr_t>(A) % 16 == 0 &&
+                         reinterpret_cast<uintptr_t>(B) % 16 == 0;
+  // other shapes of at most 2^20 multiply-adds (a 64-wide layer, a single output column):
+  // CUDA cores, where a 128-row tile pipeline would cost more than the product
+  if (!tma_shape && (long long)M * N * K <= (1LL << 20)) {
+    const long long outs = (long long)M * N;
+    k_gemm_small<<<(unsigned)((outs + 255) / 256), 256, 0, st>>>(
+        static_cast<const __nv_bfloat16*>(A), lda, transA, static_cast<const __nv_bfloat16*>(B),
+        ldb, transB, C, ldc, static_cast<__nv_bfloat16*>(C_bf16), M, N, K, alpha, beta, bias,
+        activation);
+    return cudaGetLastError() == cudaSuccess
+               ? CI_OK
+               : ci::set_last_error(CI_ERR_CUDA, "ci_gemm_bf16: small-product launch failed");
+  }
+  bool tma = tma_shape;
   const int bn_tma = N <= 64 ? 64 : N <= 128 ? 128 : 256;
   CUtensorMap ta, tb;
   tma = tma && make_tile_map(&ta, A, M, K, lda, BM) && make_tile_map(&tb, B, N, K, ldb, bn_tma);

@@ -51,6 +51,24 @@ def test_gemm_bf16(cilib, M, N, K, tA, tB):
     assert np.linalg.norm(c - ref) <= 1e-3 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("M,N,K", [(256, 1, 64), (64, 1, 256), (64, 64, 256), (256, 64, 1),
+                                   (33, 17, 5)])
+@pytest.mark.parametrize("tA,tB", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_gemm_bf16_small_products(cilib, M, N, K, tA, tB):
+    """Products of at most 2^20 multiply-adds outside the TMA shape (the plastic-strain
+    network's layers) run on the CUDA cores: same operands, accumulation and epilogue;
+    two calls give identical bits."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(M + 5 * N + 11 * K + tA + 2 * tB)
+    A = rng.standard_normal((K, M) if tA else (M, K))
+    B = rng.standard_normal((N, K) if tB else (K, N))
+    bias = rng.standard_normal(N)
+    c, ref, cb = _gemm(cilib, torch, A, B, tA, tB, bias=bias, act=1)
+    assert np.abs(c - ref).max() <= 1e-2 * max(1.0, np.abs(ref).max())
+    c2, _, _ = _gemm(cilib, torch, A, B, tA, tB, bias=bias, act=1)
+    assert np.array_equal(c, c2)
+
+
 @pytest.mark.parametrize("M,N,K", [(64, 64, 20000), (130, 5, 9000), (8, 200, 4096)])
 @pytest.mark.parametrize("tA,tB", [(1, 0), (0, 1)])
 def test_gemm_bf16_split_k(cilib, M, N, K, tA, tB):
