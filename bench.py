@@ -335,7 +335,32 @@ def run_ours(args, rank, world):
             g.close()
     if rank == 0 and args.sweep:
         line["sweep"] = run_sweep(args)
+    if rank == 0 and args.sweep and args.surrogate and args.workload == "shell":
+        s.close()
+        line["surrogate"] = surrogate_summary()
     return line
+
+
+def surrogate_summary():
+    """The learned-surrogate sweep of `--workload surrogate` in brief: runs per hour of
+    the surrogate with audit and fallback against the plain and the batched GPU solver
+    on the same 512 held-out parameter sets, its errors against the solver, and its
+    one-off cost."""
+    from cppimpact_gb300 import surrogate as sg
+    cfg = sg.Config()
+    r = sg.study(cfg)
+    rph, err = r["runs_per_hour"], r["errors"]["final_peak_disp"]
+    return {"workload": f"cube {cfg.n_cube}^3x6 tet4, {cfg.n_train} training runs, "
+                        f"{cfg.n_test} held-out parameter sets, {cfg.steps} steps",
+            "runs_per_hour": rph["surrogate"], "vs_plain_gpu": r["speedup_vs_plain_gpu"],
+            "vs_batched_gpu": rph["surrogate"] / rph["batched_solver"],
+            "plain_gpu_runs_per_hour": rph["plain_gpu_solver"],
+            "batched_gpu_runs_per_hour": rph["batched_solver"],
+            "peak_disp_err": {"p95": err["p95"], "max": err["max"],
+                              "within_2pct": 1.0 - err["frac_over_2pct"]},
+            "reruns": r["audit"]["rerun"], "fit_s": r["fit"]["wall_s"],
+            "break_even_queries": rph["break_even_queries"],
+            "gemm_tflops": r["gemm"]["square"]["tflops"]}
 
 
 def cpu_sweep_baseline(inst, nsteps, seconds_budget: float = 6.0, sample: int = 4):
@@ -526,6 +551,9 @@ def main():
                     help="steps of the GPU-vs-FP64 accuracy check on the full mesh (0: off)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep", type=int, default=1, help="also run the 256-instance batched sweep")
+    ap.add_argument("--surrogate", type=int, default=1,
+                    help="shell workload with --sweep: also run the surrogate sweep and report it "
+                         "in brief")
     ap.add_argument("--autotune", type=int, default=128,
                     help="sweep: trial steps per candidate tile shape (0 = default shape)")
     ap.add_argument("--traffic", type=float, default=None,
