@@ -14,11 +14,17 @@
 // process exits.  Host code cannot use the array's name as a device address (it is a
 // host-side shadow), so the first call on each device looks up the real address with
 // cudaGetSymbolAddress while that device is current, and passes it to the kernels.
-// Do that first call outside any stream capture.  All calls share the array and see
-// what the previous call left there: every block rewrites its own partial sums, and
-// the status word is cleared by the reduction that consumes it.  Calls that overlap
-// on the GPU (for example on two streams) race on the array and must be serialised
-// by the caller.
+// Do that first call outside any stream capture.  The cached addresses belong to the
+// device's primary context: after cudaDeviceReset (or anything else that destroys that
+// context) this entry point must not be called again in the same process.  All calls
+// share the array and see what the previous call left there: every block rewrites its
+// own partial sums, and the status word is cleared by the reduction that consumes it.
+// Calls that overlap on the GPU (for example on two streams) race on the array and
+// must be serialised by the caller.
+//
+// The connectivity is already on the device, so it cannot be validated on the host:
+// an element with a node index outside [0, num_nodes) is skipped (no load of x or u
+// through that index) and sets a status bit that turns both outputs into NaN.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -32,8 +38,9 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kMaxBlocks = CI_NOALLOC_MAX_ELEMENTS / kThreads;
 constexpr int kMaxDevices = 64;
+constexpr unsigned int kBadIndex = 4u;  // beside ci::ST_DEGENERATE (1) and ST_NONFINITE (2)
 
-// per-block partial (energy, volume) of one call; entry kMaxBlocks * 2 is unused padding
+// per-block partial (energy, volume) of one call: block b writes entries 2b and 2b + 1
 static __device__ __align__(256) double g_partials[2 * kMaxBlocks];
 static __device__ __align__(256) unsigned int g_status;
 
@@ -46,17 +53,25 @@ unsigned int* g_status_ptr[kMaxDevices] = {};
 template <int NPE>
 __global__ void __launch_bounds__(kThreads) k_energy_partials(const double* __restrict__ x,
                                                               const int* __restrict__ conn,
-                                                              const double* __restrict__ u, int E,
-                                                              ci::ElemParams p, double* partials,
+                                                              const double* __restrict__ u, int N,
+                                                              int E, ci::ElemParams p,
+                                                              double* partials,
                                                               unsigned int* status) {
   __shared__ float red[kThreads / 32];
   const int e = blockIdx.x * kThreads + threadIdx.x;
   float wint = 0.f, wp = 0.f, vol = 0.f;
-  if (e < E) {
-    float xe[NPE][3], ue[NPE][3];
-    int n[NPE];
+  int n[NPE];
+  bool ok = e < E;
+  if (ok) {
 #pragma unroll
-    for (int a = 0; a < NPE; a++) n[a] = conn[(size_t)NPE * e + a];
+    for (int a = 0; a < NPE; a++) {
+      n[a] = conn[(size_t)NPE * e + a];
+      ok = ok && (unsigned)n[a] < (unsigned)N;
+    }
+    if (!ok) atomicOr(status, kBadIndex);
+  }
+  if (ok) {
+    float xe[NPE][3], ue[NPE][3];
 #pragma unroll
     for (int a = 0; a < NPE; a++)
 #pragma unroll
@@ -77,7 +92,8 @@ __global__ void __launch_bounds__(kThreads) k_energy_partials(const double* __re
   }
 }
 
-// Fixed-order sum of the block partials; a degenerate element makes the energy NaN.
+// Fixed-order sum of the block partials; a degenerate element makes the energy NaN,
+// an out-of-range node index both outputs.
 __global__ void k_energy_reduce(const double* partials, int nblocks, unsigned int* status,
                                 double* out) {
   __shared__ double red[2][kThreads];
@@ -98,8 +114,9 @@ __global__ void k_energy_reduce(const double* partials, int nblocks, unsigned in
   }
   if (threadIdx.x == 0) {
     const unsigned int st = *status;
-    out[0] = st ? __longlong_as_double(0x7ff8000000000000ll) : red[0][0];
-    out[1] = red[1][0];
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    out[0] = st ? nan : red[0][0];
+    out[1] = (st & kBadIndex) ? nan : red[1][0];
     *status = 0u;
   }
 }
@@ -155,11 +172,11 @@ extern "C" int ci_strain_energy_noalloc(const double* d_xloc, const int* d_eleme
   const int nb = (num_elements + kThreads - 1) / kThreads;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (nodes_per_element == 4)
-    k_energy_partials<4><<<nb, kThreads, 0, st>>>(d_xloc, d_element_nodes, d_u, num_elements, p,
-                                                  partials, status);
+    k_energy_partials<4><<<nb, kThreads, 0, st>>>(d_xloc, d_element_nodes, d_u, num_nodes,
+                                                  num_elements, p, partials, status);
   else
-    k_energy_partials<10><<<nb, kThreads, 0, st>>>(d_xloc, d_element_nodes, d_u, num_elements,
-                                                   p, partials, status);
+    k_energy_partials<10><<<nb, kThreads, 0, st>>>(d_xloc, d_element_nodes, d_u, num_nodes,
+                                                   num_elements, p, partials, status);
   k_energy_reduce<<<1, kThreads, 0, st>>>(partials, nb, status, d_out);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CI_ERR_CUDA, cudaGetErrorString(e));

@@ -245,9 +245,13 @@ int ci_batch_run_peaks(ci_batch* b, int every, int max_snaps, float* peak_disp, 
  * 128-row tiles and K is long, K is split across CTAs: partial tiles go to a per-device
  * FP32 workspace (grown by cudaMalloc on first need) and are summed in a fixed order, so
  * results are deterministic; concurrent calls on different streams of one device must
- * not overlap.  C = A B^T with both operands K-major (transA = 0, transB = 1), M >= 128,
- * K >= 64, 16-byte aligned A and B and leading dimensions that are multiples of 8 runs
- * on a TMA-fed pipelined kernel; other forms on a kernel that stages operands itself. */
+ * not overlap.  Three paths, all with the same epilogue (alpha, beta C, bias, tanh,
+ * BF16 copy): C = A B^T with both operands K-major (transA = 0, transB = 1), M >= 128,
+ * N >= 16, K >= 64, 16-byte aligned A and B and leading dimensions that are multiples
+ * of 8 runs on a TMA-fed pipelined tensor-core kernel; any other form with at most
+ * 2^20 multiply-adds (M N K <= 1048576) runs on the CUDA cores, one thread per output
+ * summing the BF16 products in FP32 in K order; the remaining forms run on a
+ * tensor-core kernel that stages its operands itself. */
 int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, int ldb, int transB, float* C,
                  int ldc, void* C_bf16, int M, int N, int K, float alpha, float beta,
                  const float* bias, int activation, int* d_error, void* stream);
@@ -287,9 +291,12 @@ int ci_mlp_train(ci_mlp* m, const float* d_X, const float* d_T, int n, int batch
  * library (CI_NOALLOC_MAX_ELEMENTS / 256 blocks x 2 doubles = 256 KiB on every GPU the
  * library is used on), so at most CI_NOALLOC_MAX_ELEMENTS elements are accepted
  * (CI_ERR_TOO_LARGE beyond).  The first call on each device looks up the scratch's
- * device address and should happen before any stream capture.  Calls share the
- * scratch: calls that can overlap on the GPU race and must be serialised by the
- * caller.  A non-positive det J makes the energy NaN. */
+ * device address and should happen before any stream capture; that address is kept
+ * for the life of the device's primary context, so after cudaDeviceReset the entry
+ * point must not be called again in the same process.  Calls share the scratch:
+ * calls that can overlap on the GPU race and must be serialised by the caller.  A
+ * non-positive det J makes the energy NaN; a node index outside [0, num_nodes) makes
+ * the energy and the volume NaN (that element's loads are skipped). */
 #define CI_NOALLOC_MAX_ELEMENTS (1 << 22)
 int ci_strain_energy_noalloc(const double* d_xloc, const int* d_element_nodes, int num_nodes,
                              int num_elements, int nodes_per_element, const double* d_u, double E,
@@ -298,9 +305,9 @@ int ci_strain_energy_noalloc(const double* d_xloc, const int* d_element_nodes, i
 /* ---- timing helpers for benchmarks (CUDA events on the solver's stream) ---- */
 int ci_time_steps(ci_solver* s, int nsteps, float* ms);
 /* Runs nsteps steps launching each kernel between CUDA events and returns mean device
- * durations (ms): fused path out[0] = the step kernel, out[1] = the end-of-call
- * boundary finalise divided by nsteps; two-kernel path out[0] = element kernel,
- * out[1] = node kernel. */
+ * durations (ms): fused path out[0] = the step kernel, out[1] = the one end-of-call
+ * finalise divided by nsteps (its share per step); two-kernel path out[0] = element
+ * kernel, out[1] = node kernel. */
 int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms);
 /* Kernel launches one step issues (for launch accounting). */
 int ci_launches_per_step(const ci_solver* s);

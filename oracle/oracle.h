@@ -138,6 +138,10 @@ void orc_destroy(orc_solver* s);
 /* x = X + pos, v = vel; mass; a0 from zero increment; v += dt/2 a0 (dynamics.h:440-463) */
 int orc_initialize(orc_solver* s, const double pos[3], const double vel[3], double dt);
 int orc_step(orc_solver* s, int nsteps);
+/* Threads of orc_step's loops (default 1).  The results do not depend on it: each
+ * node's force is summed over its elements in element order, as with one thread, and
+ * the work terms over fixed blocks of elements in block order. */
+int orc_set_threads(orc_solver* s, int nthreads);
 /* Any output may be NULL.  x, v: [3N]; mass [N]; sigma [E*nq*6]; epbar [E*nq];
  * energy [ORC_E_COUNT]; contact [N]: bit0 in contact at the last step, bit1 ever. */
 int orc_get(const orc_solver* s, double* x, double* v, double* mass, double* sigma,

@@ -63,6 +63,7 @@ def lib():
         L.orc_destroy.argtypes = [C.c_void_p]
         L.orc_initialize.argtypes = [C.c_void_p, _dp, _dp, C.c_double]
         L.orc_step.argtypes = [C.c_void_p, C.c_int]
+        L.orc_set_threads.argtypes = [C.c_void_p, C.c_int]
         L.orc_get.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(C.c_ubyte)]
         L.orc_j2_update.argtypes = [C.c_double] * 4 + [_dp, _dp, _dp]
         L.orc_ref_solve.argtypes = [C.POINTER(OrcMesh), C.POINTER(OrcRefParams), _dp, _dp,
@@ -175,7 +176,9 @@ def j2_update(E, nu, sy0, H, deps, sigma, epbar):
 class Solver:
     """The FP64 run of the GB300 solver's formulation."""
 
-    def __init__(self, xloc, conn, p: OrcParams):
+    def __init__(self, xloc, conn, p: OrcParams, nthreads: int = 1):
+        """nthreads > 1 (0 = all host cores) runs the step's loops in parallel; the
+        results are the same bits for any thread count."""
         self._h = _MeshHold(xloc, conn)
         self.p = p
         self.N = self._h.x.size // 3
@@ -183,6 +186,9 @@ class Solver:
         self.nq = 1 if self.npe == 4 else 4
         self._s = lib().orc_create(C.byref(self._h.s), C.byref(p))
         assert self._s
+        nthreads = nthreads or os.cpu_count() or 1
+        if nthreads > 1:
+            assert lib().orc_set_threads(self._s, int(nthreads)) == 0
 
     def __del__(self):
         if getattr(self, "_s", None):

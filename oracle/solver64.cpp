@@ -16,8 +16,14 @@
 // Quadrature: 1 point for tet4 (B is constant, so K_e equals the reference's 5-point
 // K_e up to its truncated weights), 4-point Gauss for tet10 (degree 2, exact for the
 // straight-sided K_e and row-sum mass).
+#include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
+#include <memory>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "oracle.h"
@@ -199,6 +205,120 @@ extern "C" int orc_lumped_mass(const orc_mesh* m, const orc_params* p, const dou
   return 0;
 }
 
+namespace {
+
+// One element's internal force fe[3 npe] at positions x with increment du, its QP
+// states updated in place (sigma/epbar may be NULL: zero stored state, not written),
+// and its internal-work and plastic-dissipation increments added to *wint / *wp in
+// QP order.
+void element_force(int npe, const Rule& r, const Elastic& el, const orc_params* p, bool j2,
+                   const int* nodes, const double* x, const double* du, const double* sigma_in,
+                   const double* epbar_in, double* sigma_out, double* epbar_out, size_t e,
+                   double* fe, double* wint, double* wp) {
+  double xe[30], de[30], dNdx[30];
+  gather3(npe, nodes, x, xe);
+  gather3(npe, nodes, du, de);
+  for (int i = 0; i < 3 * npe; i++) fe[i] = 0.0;
+  for (int q = 0; q < r.nq; q++) {
+    const double detJ = qp_geometry(npe, r.pt[q], xe, dNdx);
+    const double wd = r.w[q] * detJ;
+    double L[9] = {0};
+    for (int i = 0; i < npe; i++)
+      for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) L[3 * a + b] += de[3 * i + a] * dNdx[3 * i + b];
+    const double deps[6] = {L[0], L[4], L[8], L[1] + L[3], L[5] + L[7], L[2] + L[6]};
+    const size_t qi = e * r.nq + q;
+    double s[6] = {0, 0, 0, 0, 0, 0}, s0[6] = {0, 0, 0, 0, 0, 0}, ep = 0.0;
+    if (j2 && sigma_in) std::memcpy(s, sigma_in + 6 * qi, sizeof(s));
+    if (j2 && epbar_in) ep = epbar_in[qi];
+    std::memcpy(s0, s, sizeof(s));
+    const double ep0 = ep;
+    j2_update(el, p->sigma_y0, p->H, deps, s, &ep, j2);
+    if (sigma_out) std::memcpy(sigma_out + 6 * qi, s, sizeof(s));
+    if (epbar_out) epbar_out[qi] = ep;
+    double wq = 0.0;
+    for (int k = 0; k < 6; k++) wq += 0.5 * (s0[k] + s[k]) * deps[k];
+    *wint += wd * wq;
+    *wp += wd * (p->sigma_y0 + p->H * ep) * (ep - ep0);
+    const double S[9] = {s[0], s[3], s[5], s[3], s[1], s[4], s[5], s[4], s[2]};
+    for (int i = 0; i < npe; i++)
+      for (int a = 0; a < 3; a++)
+        fe[3 * i + a] += wd * (S[3 * a + 0] * dNdx[3 * i + 0] + S[3 * a + 1] * dNdx[3 * i + 1] +
+                               S[3 * a + 2] * dNdx[3 * i + 2]);
+  }
+}
+
+// Fork-join pool for the solver's loops: run(fn) calls fn(t) on threads t = 0..n-1
+// (t = 0 on the caller) and returns when all are done.
+class Pool {
+ public:
+  explicit Pool(int n) : n_(n < 1 ? 1 : n) {
+    for (int t = 1; t < n_; t++) th_.emplace_back([this, t] { worker(t); });
+  }
+  ~Pool() {
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      stop_ = true;
+      gen_++;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  int size() const { return n_; }
+  void run(const std::function<void(int)>& fn) {
+    if (n_ == 1) {
+      fn(0);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      fn_ = &fn;
+      pending_ = n_ - 1;
+      gen_++;
+    }
+    cv_.notify_all();
+    fn(0);
+    std::unique_lock<std::mutex> l(mu_);
+    done_.wait(l, [this] { return pending_ == 0; });
+  }
+
+ private:
+  void worker(int t) {
+    unsigned long long seen = 0;
+    for (;;) {
+      const std::function<void(int)>* fn;
+      {
+        std::unique_lock<std::mutex> l(mu_);
+        cv_.wait(l, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (stop_) return;
+        fn = fn_;
+      }
+      (*fn)(t);
+      std::lock_guard<std::mutex> l(mu_);
+      if (--pending_ == 0) done_.notify_one();
+    }
+  }
+  int n_;
+  std::vector<std::thread> th_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* fn_ = nullptr;
+  int pending_ = 0;
+  unsigned long long gen_ = 0;
+  bool stop_ = false;
+};
+
+// contiguous share [b, e) of n items for thread t of T
+inline void share(size_t n, int t, int T, size_t* b, size_t* e) {
+  *b = n * (size_t)t / (size_t)T;
+  *e = n * (size_t)(t + 1) / (size_t)T;
+}
+
+constexpr size_t kBlock = 1024;  // elements per work-sum block (fixed: thread-count independent)
+
+}  // namespace
+
 extern "C" int orc_internal_force(const orc_mesh* m, const orc_params* p, const double* x,
                                   const double* du, const double* sigma_in,
                                   const double* epbar_in, double* f, double* sigma_out,
@@ -210,39 +330,11 @@ extern "C" int orc_internal_force(const orc_mesh* m, const orc_params* p, const 
   const bool j2 = p->mode == ORC_J2;
   std::memset(f, 0, sizeof(double) * 3 * m->num_nodes);
   double Wint = 0.0, Wp = 0.0;
-  double xe[30], de[30], dNdx[30];
+  double fe[30];
   for (int e = 0; e < m->num_elements; e++) {
     const int* nodes = m->conn + (size_t)npe * e;
-    gather3(npe, nodes, x, xe);
-    gather3(npe, nodes, du, de);
-    double fe[30] = {0};
-    for (int q = 0; q < r.nq; q++) {
-      const double detJ = qp_geometry(npe, r.pt[q], xe, dNdx);
-      const double wd = r.w[q] * detJ;
-      double L[9] = {0};
-      for (int i = 0; i < npe; i++)
-        for (int a = 0; a < 3; a++)
-          for (int b = 0; b < 3; b++) L[3 * a + b] += de[3 * i + a] * dNdx[3 * i + b];
-      const double deps[6] = {L[0], L[4], L[8], L[1] + L[3], L[5] + L[7], L[2] + L[6]};
-      const size_t qi = (size_t)e * r.nq + q;
-      double s[6] = {0, 0, 0, 0, 0, 0}, s0[6] = {0, 0, 0, 0, 0, 0}, ep = 0.0;
-      if (j2 && sigma_in) std::memcpy(s, sigma_in + 6 * qi, sizeof(s));
-      if (j2 && epbar_in) ep = epbar_in[qi];
-      std::memcpy(s0, s, sizeof(s));
-      const double ep0 = ep;
-      j2_update(el, p->sigma_y0, p->H, deps, s, &ep, j2);
-      if (sigma_out) std::memcpy(sigma_out + 6 * qi, s, sizeof(s));
-      if (epbar_out) epbar_out[qi] = ep;
-      double wq = 0.0;
-      for (int k = 0; k < 6; k++) wq += 0.5 * (s0[k] + s[k]) * deps[k];
-      Wint += wd * wq;
-      Wp += wd * (p->sigma_y0 + p->H * ep) * (ep - ep0);
-      const double S[9] = {s[0], s[3], s[5], s[3], s[1], s[4], s[5], s[4], s[2]};
-      for (int i = 0; i < npe; i++)
-        for (int a = 0; a < 3; a++)
-          fe[3 * i + a] += wd * (S[3 * a + 0] * dNdx[3 * i + 0] + S[3 * a + 1] * dNdx[3 * i + 1] +
-                                 S[3 * a + 2] * dNdx[3 * i + 2]);
-    }
+    element_force(npe, r, el, p, j2, nodes, x, du, sigma_in, epbar_in, sigma_out, epbar_out,
+                  (size_t)e, fe, &Wint, &Wp);
     for (int i = 0; i < npe; i++)
       for (int a = 0; a < 3; a++) f[3 * (size_t)nodes[i] + a] += fe[3 * i + a];
   }
@@ -258,30 +350,38 @@ struct orc_solver {
   orc_params p;
   int nq;
   std::vector<int> conn;
-  std::vector<double> X0, X, x, v, a, mass, sigma, epbar, f, du;
+  std::vector<double> X0, X, x, v, a, mass, sigma, epbar, f, du, pos;
   std::vector<unsigned char> contact;
   double dt = 0.0, Wint = 0.0, Wp = 0.0, KE0 = 0.0, Phi0 = 0.0;
+  // threaded step: per-element forces, per-block work sums, node -> (element, local
+  // node) incidence in element order (so every node's force is summed in the order
+  // of the one-thread loop)
+  std::unique_ptr<Pool> pool;
+  std::vector<double> fe_all, block_work;
+  std::vector<long long> inc_row;
+  std::vector<int> inc;
 };
 
 namespace {
 
-// Wall and gravity on the accelerations; contact potential 1/2 k d^2 of the
-// penetration at p = x + du (planar generalisation of include/wall.h:37-43).
-double apply_wall(orc_solver* s, const double* pos, double* acc, bool flag) {
+// Wall and gravity on the accelerations of nodes [i0, i1); contact potential 1/2 k d^2
+// of the penetration at p = x + du (planar generalisation of include/wall.h:37-43).
+double apply_wall(orc_solver* s, const double* pos, double* acc, bool flag, size_t i0,
+                  size_t i1) {
   const orc_params& P = s->p;
   double phi = 0.0;
-  for (int i = 0; i < s->m.num_nodes; i++) {
-    const double* q = pos + 3 * (size_t)i;
+  for (size_t i = i0; i < i1; i++) {
+    const double* q = pos + 3 * i;
     const double d = P.wall_normal[0] * q[0] + P.wall_normal[1] * q[1] + P.wall_normal[2] * q[2] -
                      P.wall_offset;
     if (flag) s->contact[i] &= 2;
     if (d < 0.0) {
       const double c = -d * P.wall_stiffness / s->mass[i];
-      for (int k = 0; k < 3; k++) acc[3 * (size_t)i + k] += c * P.wall_normal[k];
+      for (int k = 0; k < 3; k++) acc[3 * i + k] += c * P.wall_normal[k];
       phi += 0.5 * P.wall_stiffness * d * d;
       if (flag) s->contact[i] |= 3;
     }
-    for (int k = 0; k < 3; k++) acc[3 * (size_t)i + k] += P.gravity[k];
+    for (int k = 0; k < 3; k++) acc[3 * i + k] += P.gravity[k];
   }
   return phi;
 }
@@ -295,6 +395,16 @@ double contact_potential(const orc_solver* s, const double* pos) {
     if (d < 0.0) phi += 0.5 * s->p.wall_stiffness * d * d;
   }
   return phi;
+}
+
+void build_incidence(orc_solver* s) {
+  const size_t N = s->m.num_nodes, E = s->m.num_elements, npe = s->m.nodes_per_element;
+  s->inc_row.assign(N + 1, 0);
+  for (size_t k = 0; k < E * npe; k++) s->inc_row[s->conn[k] + 1]++;
+  for (size_t i = 0; i < N; i++) s->inc_row[i + 1] += s->inc_row[i];
+  s->inc.resize(E * npe);
+  std::vector<long long> fill(s->inc_row.begin(), s->inc_row.end() - 1);
+  for (size_t k = 0; k < E * npe; k++) s->inc[fill[s->conn[k]]++] = (int)k;  // element order
 }
 
 }  // namespace
@@ -315,14 +425,22 @@ extern "C" orc_solver* orc_create(const orc_mesh* m, const orc_params* p) {
   s->a.assign(3 * N, 0.0);
   s->f.assign(3 * N, 0.0);
   s->du.assign(3 * N, 0.0);
+  s->pos.assign(3 * N, 0.0);
   s->mass.assign(N, 0.0);
   s->sigma.assign(6 * E * s->nq, 0.0);
   s->epbar.assign(E * s->nq, 0.0);
   s->contact.assign(N, 0);
+  s->pool.reset(new Pool(1));
   return s;
 }
 
 extern "C" void orc_destroy(orc_solver* s) { delete s; }
+
+extern "C" int orc_set_threads(orc_solver* s, int nthreads) {
+  if (nthreads < 1) return -1;
+  s->pool.reset(new Pool(nthreads));
+  return 0;
+}
 
 extern "C" int orc_initialize(orc_solver* s, const double pos[3], const double vel[3], double dt) {
   const int N = s->m.num_nodes;
@@ -343,31 +461,72 @@ extern "C" int orc_initialize(orc_solver* s, const double pos[3], const double v
     s->KE0 += 0.5 * s->mass[i] * (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
   // a0 from a zero increment: f_int = 0 for zero stored stress (include/dynamics.h:454-463)
   std::fill(s->a.begin(), s->a.end(), 0.0);
-  s->Phi0 = apply_wall(s, s->x.data(), s->a.data(), true);
+  s->Phi0 = apply_wall(s, s->x.data(), s->a.data(), true, 0, (size_t)N);
   for (int i = 0; i < 3 * N; i++) s->v[i] += 0.5 * dt * s->a[i];
   return 0;
 }
 
+// One step per iteration: du = dt v; element forces (J2 update) in parallel over
+// elements; each node's force summed over its elements in element order; a = -f/m +
+// wall + gravity at x + du; x += du; v += dt a.  The result does not depend on the
+// thread count: forces are summed per node in the one-thread loop's order and the
+// work terms over fixed blocks of kBlock elements, in block order.
 extern "C" int orc_step(orc_solver* s, int nsteps) {
-  const int N = s->m.num_nodes;
+  const size_t N = s->m.num_nodes, E = s->m.num_elements;
+  const int npe = s->m.nodes_per_element;
   const double dt = s->dt;
+  const Rule r = rule_for(npe);
+  const Elastic el = lame(s->p.E, s->p.nu);
+  const bool j2 = s->p.mode == ORC_J2;
+  const size_t nblocks = (E + kBlock - 1) / kBlock;
+  if (s->inc.empty()) build_incidence(s);
+  s->fe_all.resize(E * 3 * npe);
+  s->block_work.resize(2 * nblocks);
+  Pool& pool = *s->pool;
+  const int T = pool.size();
   for (int it = 0; it < nsteps; it++) {
-    for (int i = 0; i < 3 * N; i++) s->du[i] = dt * s->v[i];
-    double work[2];
-    const bool j2 = s->p.mode == ORC_J2;
-    orc_internal_force(&s->m, &s->p, s->x.data(), s->du.data(), j2 ? s->sigma.data() : nullptr,
-                       j2 ? s->epbar.data() : nullptr, s->f.data(), j2 ? s->sigma.data() : nullptr,
-                       j2 ? s->epbar.data() : nullptr, work);
-    s->Wint += work[0];
-    s->Wp += work[1];
-    for (int i = 0; i < N; i++)
-      for (int k = 0; k < 3; k++) s->a[3 * i + k] = -s->f[3 * i + k] / s->mass[i];
-    std::vector<double> pos(3 * (size_t)N);
-    for (int i = 0; i < 3 * N; i++) pos[i] = s->x[i] + s->du[i];
-    apply_wall(s, pos.data(), s->a.data(), true);
-    for (int i = 0; i < 3 * N; i++) {
-      s->x[i] = pos[i];
-      s->v[i] += dt * s->a[i];
+    pool.run([&](int t) {
+      size_t b, e;
+      share(3 * N, t, T, &b, &e);
+      for (size_t i = b; i < e; i++) s->du[i] = dt * s->v[i];
+    });
+    pool.run([&](int t) {
+      for (size_t blk = t; blk < nblocks; blk += T) {
+        double wi = 0.0, wpl = 0.0;
+        const size_t e1 = std::min(E, (blk + 1) * kBlock);
+        for (size_t e = blk * kBlock; e < e1; e++)
+          element_force(npe, r, el, &s->p, j2, s->conn.data() + (size_t)npe * e, s->x.data(),
+                        s->du.data(), j2 ? s->sigma.data() : nullptr,
+                        j2 ? s->epbar.data() : nullptr, j2 ? s->sigma.data() : nullptr,
+                        j2 ? s->epbar.data() : nullptr, e, s->fe_all.data() + 3 * npe * e, &wi,
+                        &wpl);
+        s->block_work[2 * blk] = wi;
+        s->block_work[2 * blk + 1] = wpl;
+      }
+    });
+    pool.run([&](int t) {
+      size_t b, e;
+      share(N, t, T, &b, &e);
+      for (size_t i = b; i < e; i++) {
+        double f[3] = {0.0, 0.0, 0.0};
+        for (long long k = s->inc_row[i]; k < s->inc_row[i + 1]; k++) {
+          const double* fe = s->fe_all.data() + 3 * (size_t)s->inc[k];
+          for (int c = 0; c < 3; c++) f[c] += fe[c];
+        }
+        for (int c = 0; c < 3; c++) {
+          s->a[3 * i + c] = -f[c] / s->mass[i];
+          s->pos[3 * i + c] = s->x[3 * i + c] + s->du[3 * i + c];
+        }
+      }
+      apply_wall(s, s->pos.data(), s->a.data(), true, b, e);
+      for (size_t i = 3 * b; i < 3 * e; i++) {
+        s->x[i] = s->pos[i];
+        s->v[i] += dt * s->a[i];
+      }
+    });
+    for (size_t blk = 0; blk < nblocks; blk++) {
+      s->Wint += s->block_work[2 * blk];
+      s->Wp += s->block_work[2 * blk + 1];
     }
   }
   return 0;

@@ -120,7 +120,7 @@ def test_inp_reader_errors(cilib, tmp_path):
     assert mesh.load_mesh(str(p)) == 1
 
 
-REF_INPUT = "/root/reference/input"
+REF_INPUT = os.path.join(os.environ.get("CPPIMPACT_REF_ROOT") or os.path.join(os.path.dirname(ROOT), "reference"), "input")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_INPUT), reason="reference checkout not present")

@@ -12,7 +12,8 @@ import pytest
 from conftest import ROOT
 from cppimpact_gb300 import meshgen as mg
 
-REF = "/root/reference"
+# the reference checkout: $CPPIMPACT_REF_ROOT, else a "reference" directory beside the repo
+REF = os.environ.get("CPPIMPACT_REF_ROOT") or os.path.join(os.path.dirname(ROOT), "reference")
 INC = os.path.join(ROOT, "include", "cppimpact")
 LIBDIR = os.path.join(ROOT, "cppimpact_gb300")
 STUB = os.path.join(ROOT, "oracle", "stub")
@@ -93,3 +94,42 @@ def test_reference_style_driver_runs_on_gpu(cilib, oracle, tmp_path):
     assert sorted(os.listdir(out)) == ["simulation_0.vtk", "simulation_100.vtk"]
     W = float(r.stdout.split("W ")[1].split()[0])
     assert W == pytest.approx(84161.61854712779, rel=1e-5)
+
+
+GEMV = r"""
+#include <cstdio>
+#include "include/cppimpact_blas.h"
+int main() {
+  const double a[6] = {1, 2, 3, 4, 5, 6}, x3[3] = {1, -1, 2}, x2[2] = {0.5, 3};
+  double y[3] = {1, 2, 0};
+  cppimpact_gemv<double, MatOp::NoTrans>(2, 3, 2.0, a, x3, 0.5, y);
+  double z[3] = {1, 2, 3};
+  cppimpact_gemv<double, MatOp::Trans>(2, 3, -1.0, a, x2, 0.25, z);
+  printf("%.17g %.17g %.17g %.17g %.17g\n", y[0], y[1], z[0], z[1], z[2]);
+  return 0;
+}
+"""
+
+
+def _run_gemv(tmp, name, include_dir):
+    work = tmp / name
+    work.mkdir()
+    os.symlink(include_dir, work / "include")
+    (work / "g.cpp").write_text(GEMV)
+    exe = work / "g"
+    r = subprocess.run(["g++", "-std=c++17", "-O0", f"-I{work}",
+                        str(work / "g.cpp"), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return [float(t) for t in subprocess.run([str(exe)], capture_output=True, text=True,
+                                              check=True).stdout.split()]
+
+
+def test_gemv_keeps_reference_semantics(tmp_path):
+    """cppimpact_gemv adds beta to y and accumulates alpha op(A) x into y
+    (include/cppimpact_blas.h:9-29), which differs from BLAS's beta*y unless beta = 0."""
+    got = _run_gemv(tmp_path, "dropin", INC)
+    # y_i + beta + alpha (A x)_i ; z_i + beta + alpha (A^T x)_i
+    assert got == [1 + 0.5 + 2 * (1 - 2 + 6), 2 + 0.5 + 2 * (4 - 5 + 12),
+                   1 + 0.25 - (0.5 + 12), 2 + 0.25 - (1 + 15), 3 + 0.25 - (1.5 + 18)]
+    if os.path.isfile(os.path.join(REF, "include", "cppimpact_blas.h")):
+        assert got == _run_gemv(tmp_path, "ref", os.path.join(REF, "include"))

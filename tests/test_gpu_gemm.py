@@ -56,8 +56,8 @@ def test_gemm_bf16(cilib, M, N, K, tA, tB):
 @pytest.mark.parametrize("tA,tB", [(0, 0), (1, 0), (0, 1), (1, 1)])
 def test_gemm_bf16_small_products(cilib, M, N, K, tA, tB):
     """Products of at most 2^20 multiply-adds outside the TMA shape (the plastic-strain
-    network's layers) run on the CUDA cores: same operands, accumulation and epilogue;
-    two calls give identical bits."""
+    network's layers) run on the CUDA cores: same operands, accumulation and epilogue
+    (beta C added, bias, tanh, BF16 copy of C); two calls give identical bits."""
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(M + 5 * N + 11 * K + tA + 2 * tB)
     A = rng.standard_normal((K, M) if tA else (M, K))
@@ -67,6 +67,13 @@ def test_gemm_bf16_small_products(cilib, M, N, K, tA, tB):
     assert np.abs(c - ref).max() <= 1e-2 * max(1.0, np.abs(ref).max())
     c2, _, _ = _gemm(cilib, torch, A, B, tA, tB, bias=bias, act=1)
     assert np.array_equal(c, c2)
+    # beta != 0 reads C before writing it; the BF16 copy is C rounded to nearest
+    # (relative error at most 2^-8 for a 8-bit significand)
+    C0 = rng.standard_normal((M, N))
+    for act in (0, 1):
+        c, ref, cb = _gemm(cilib, torch, A, B, tA, tB, bias=bias, act=act, beta=0.75, C0=C0)
+        assert np.abs(c - ref).max() <= 1e-2 * max(1.0, np.abs(ref).max())
+        assert np.all(np.abs(cb - c) <= 2.0 ** -8 * np.abs(c))
 
 
 @pytest.mark.parametrize("M,N,K", [(64, 64, 20000), (130, 5, 9000), (8, 200, 4096)])

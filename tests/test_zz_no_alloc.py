@@ -57,3 +57,50 @@ def test_noalloc_rejects_oversize(cilib):
                                     C.c_void_p(16), E, NU, C.c_void_p(16), None)
     assert rc == -8
     assert b"CI_NOALLOC_MAX_ELEMENTS" in L.ci_last_error()
+
+
+def _call(cilib, torch, xloc, conn, u):
+    """One call through the C ABI on device buffers made from host arrays; returns
+    (energy, volume)."""
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    dx = torch.tensor(np.ascontiguousarray(xloc).reshape(-1), dtype=torch.float64, device=dev)
+    dc = torch.tensor(np.ascontiguousarray(conn).reshape(-1), dtype=torch.int32, device=dev)
+    du = torch.tensor(np.ascontiguousarray(u).reshape(-1), dtype=torch.float64, device=dev)
+    out = torch.full((2,), -1.0, dtype=torch.float64, device=dev)
+    L = cilib.lib()
+    rc = L.ci_strain_energy_noalloc(dx.data_ptr(), dc.data_ptr(), xloc.shape[0], conn.shape[0],
+                                    conn.shape[1], du.data_ptr(), E, NU, out.data_ptr(),
+                                    C.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    assert rc == 0, L.ci_last_error()
+    torch.cuda.synchronize(dev)
+    return out.cpu().tolist()
+
+
+def test_noalloc_status_word_is_cleared_between_calls(cilib):
+    """The status word is the one piece of state the shared scratch carries from call to
+    call.  An inverted element makes that call's energy NaN; an out-of-range node index
+    (caught in the kernel: the element's loads are skipped) makes both outputs NaN; the
+    next call on a valid mesh must again match ci_strain_energy."""
+    torch = pytest.importorskip("torch")
+    m = mg.cube(3, 1)
+    g = m.xloc[:, 0]
+    u = np.stack([0.01 * g, -0.01 * NU * g, -0.01 * NU * g], axis=1)
+    s = cilib.Solver(m.xloc, m.conn, E=E, nu=NU, rho=2700.0, mode=cilib.MODE_REFCOMPAT)
+    W_ref, V_ref = s.strain_energy(u)
+    s.close()
+
+    inverted = m.conn.copy()
+    inverted[5, [1, 2]] = inverted[5, [2, 1]]  # swapping two corners makes det J < 0
+    W, V = _call(cilib, torch, m.xloc, inverted, u)
+    assert np.isnan(W) and np.isfinite(V)
+    W, V = _call(cilib, torch, m.xloc, m.conn, u)
+    assert W == pytest.approx(W_ref, rel=1e-5) and V == pytest.approx(V_ref, rel=1e-5)
+
+    for bad in (m.num_nodes, -1):
+        wrong = m.conn.copy()
+        wrong[7, 3] = bad
+        W, V = _call(cilib, torch, m.xloc, wrong, u)
+        assert np.isnan(W) and np.isnan(V)
+        W, V = _call(cilib, torch, m.xloc, m.conn, u)
+        assert W == pytest.approx(W_ref, rel=1e-5) and V == pytest.approx(V_ref, rel=1e-5)
