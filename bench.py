@@ -11,12 +11,23 @@ step (element internal force + J2 update, force assembly, contact, central-diffe
 update) over the whole mesh; the working set (~0.3 GB per step) exceeds L2, so no
 flush is needed between steps.
 
-Our arm prints one JSON line with value (device-resident, CUDA events on the solver's
-stream), e2e (through the C ABI with host buffers and the copies inside the timed
-region), the roofline of the dominant kernel, the CPU baseline and sampled clocks.
-The reference arm (--impl reference) times the reference's CPU algorithm -- the
-oracle's restatement of it, since the reference's compiled code cannot travel -- with
-all host threads on a bounded sample of the same workload.
+Timing: after --preroll untimed steps (the impact under way, contact established) and
+W warm-up steps, a window of K steps is timed with CUDA events on the solver's stream
+and repeated back to back until at least --min-timed-s of device time is covered (the
+clock sampler needs a region of that length); `value` is the median window.  At 5 m/s
+the shell stays elastic (peak von Mises stress about 0.4 of yield), so the same mesh at
+--plastic-speed (40 m/s, where a few per cent of the Gauss points yield) is timed the
+same way and reported as `j2_active`.
+
+Our arm prints one JSON line with value (device-resident), e2e (through the C ABI with
+host buffers and the copies inside the timed region), the roofline of the dominant
+kernel, the CPU baseline (the reference algorithm on one core and on all cores), the
+accuracy against the FP64 run of the same formulation at both speeds, and sampled
+clocks.  The reference arm (--impl reference) times the reference's CPU algorithm --
+the oracle's restatement of it, bitwise identical to the compiled reference on the
+golden fixtures, since the reference's compiled code cannot travel -- with all host
+threads on whole-mesh steps (a sample of the elements when W + K steps would not fit
+its time budget).
 
 Under torchrun (N > 1) every rank runs its own replica (the step does not shard
 across GPUs without a halo exchange; replicas only) and rank 0 reports the aggregate.
@@ -162,52 +173,49 @@ def max_over_ranks(x: float, world: int) -> float:
     return float(t.item())
 
 
-def cpu_baseline(m, setup, seconds_budget: float = 15.0, threads: int | None = None):
-    """The reference's CPU algorithm (restated in oracle/ref_port.cpp: 5-point K_e,
-    dense gemv, row-sum mass, z-wall) on a bounded sample: whole solver steps over the
-    first elements of the mesh, all host threads."""
+def _ref_setup(m, setup):
+    """Reference-law parameters (5-point K_e, row-sum mass, wall along the impact
+    normal, include/dynamics_kernels.h:8-169) and one step's increment dt v0."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py as op
-    threads = threads or os.cpu_count() or 1
+    rp = op.ref_params(MAT["E"], MAT["nu"], MAT["rho"], setup["wall_offset"],
+                       setup["wall_stiffness"], 1)
+    dof = np.tile(np.asarray(setup["vel"], dtype=np.float64) * setup["dt"], m.num_nodes)
+    return op, rp, dof
+
+
+def cpu_baseline(m, setup, threads: int | None = None):
+    """The reference's CPU algorithm (restated in oracle/ref_port.cpp: 5-point K_e, dense
+    gemv, scatter, stress/strain output, row-sum mass assembled once, wall, gravity) over
+    whole-mesh steps: all host threads (element loop split in contiguous ranges) and one
+    thread (the reference itself is single-threaded)."""
+    op, rp, dof = _ref_setup(m, setup)
+    cores = os.cpu_count() or 1
+    threads = threads or cores
     E = m.num_elements
-    # probe: one step on a small slice sizes the sample to the budget
-    def run(ne, nsteps):
-        conn = m.conn[:ne]
-        used = np.unique(conn)
-        remap = np.full(m.num_nodes, -1, np.int32)
-        remap[used] = np.arange(used.size, dtype=np.int32)
-        x = m.xloc[used]
-        c = remap[conn]
-        rp = op.ref_params(MAT["E"], MAT["nu"], MAT["rho"], setup["wall_offset"],
-                           setup["wall_stiffness"], 1)
-        t0 = time.perf_counter()
-        op.ref_solve(x, c, rp, setup["vel"], setup["dt"], (nsteps - 1) * setup["dt"] + 0.5 * setup["dt"],
-                     nthreads=threads)
-        return time.perf_counter() - t0
-    ne = min(E, 4096)
-    t = run(ne, 1)
-    per_elem_step = t / (ne * 2)  # initial update + one step
-    ne = int(min(E, max(ne, seconds_budget / 2 / per_elem_step)))
-    nsteps = 1
-    t = run(ne, nsteps)
-    value = ne * (nsteps + 1) / t
-    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{ne} of {E} elements (first in mesh order), {nsteps + 1} updates "
-                      f"(initial + {nsteps} step), RefCompat 5-point K_e, {t:.1f} s"}
+    t_all = op.ref_time_steps(m.xloc, m.conn, rp, dof, 2, nthreads=threads, warmup=1)
+    t_one = op.ref_time_steps(m.xloc, m.conn, rp, dof, 1, nthreads=1)
+    return {"value": 2 * E / t_all, "unit": UNIT, "cores": cores, "cores_used": threads,
+            "kind": "port",
+            "sample": f"whole mesh ({E} elements), 2 steps after 1 warm-up step, reference "
+                      f"force law (5-point K_e, gemv, stress/strain output), {t_all:.1f} s",
+            "single_core": {"value": E / t_one, "cores_used": 1,
+                            "sample": f"whole mesh, 1 step, {t_one:.1f} s"}}
 
 
 def fp64_accuracy(m, setup, gpu, nsteps):
     """Error of the GPU run against the FP64 run of the same formulation (oracle/
-    solver64.cpp, one host thread) on the full mesh after nsteps steps from the same
+    solver64.cpp, all host threads) on the full mesh after nsteps steps from the same
     start: relative L2 of the displacement, of the velocity change and of the plastic
-    strain, and whether the contact-node sets agree."""
+    strain, the fraction of Gauss points that yielded, and whether the contact-node sets
+    agree."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py as op
     par = op.params(MAT["E"], MAT["nu"], MAT["rho"], MAT["sigma_y0"], MAT["H"], mode=op.J2,
                     lumping=op.LUMP_HRZ, wall_normal=setup["wall_normal"],
                     wall_offset=setup["wall_offset"], wall_stiffness=setup["wall_stiffness"])
     t0 = time.perf_counter()
-    o = op.Solver(m.xloc, m.conn, par)
+    o = op.Solver(m.xloc, m.conn, par, nthreads=0)
     o.initialize(setup["vel"], setup["dt"])
     o.step(nsteps)
     ref = o.get()
@@ -223,15 +231,14 @@ def fp64_accuracy(m, setup, gpu, nsteps):
             "dv_rel_l2": rel(gpu["v"] - v0, ref["v"] - v0),
             "epbar_rel_l2": rel(gpu["epbar"], ref["epbar"]) if ref["epbar"].max() > 0 else None,
             "epbar_max": float(ref["epbar"].max()),
+            "yielded_qp_frac": float((ref["epbar"] > 0).mean()),
             "contact_nodes": int(ever_ref.sum()),
             "contact_sets_equal": bool(np.array_equal(ever, ever_ref)),
             "fp64_seconds": round(t, 1)}
 
 
-def run_ours(args, rank, world):
+def make_solver(m, setup, args):
     from cppimpact_gb300 import api
-    m, setup, desc = workload(args.workload)
-    N, E, npe = m.num_nodes, m.num_elements, m.npe
     s = api.Solver(m.xloc, m.conn, **MAT, mode=api.MODE_J2, lumping=api.LUMP_HRZ,
                    step_kernel=args.step_kernel, chunk_elements=args.chunk_elements,
                    chunk_nodes=args.chunk_nodes, block_threads=args.block_threads,
@@ -241,13 +248,45 @@ def run_ours(args, rank, world):
                    device=int(os.environ.get("LOCAL_RANK", "0")))
     s.initialize(setup["vel"])
     s.start(setup["dt"])
+    return s
+
+
+def timed_window(s, args, world, min_ms):
+    """Device time of K steps (CUDA events on the solver's stream, one ci_step call:
+    K step launches and the end-of-call completion), repeated back to back with a
+    barrier around each repetition until at least min_ms of device time is covered (so
+    the sampled clocks see the region); max over ranks, median over repetitions."""
+    first = s.time_steps(args.steps)
+    reps = [first]
+    n = max(3, int(np.ceil(min_ms / max(max_over_ranks(first, world), 1e-6))))
+    for _ in range(n - 1):
+        barrier(world)
+        reps.append(s.time_steps(args.steps))
+        barrier(world)
+    med = max_over_ranks(statistics.median(reps), world)
+    return med, reps
+
+
+def yield_fraction(s):
+    ep = s.state(("epbar",))["epbar"]
+    return float((ep > 0).mean()), float(ep.max())
+
+
+def run_ours(args, rank, world):
+    m, setup, desc = workload(args.workload)
+    N, E, npe = m.num_nodes, m.num_elements, m.npe
+    s = make_solver(m, setup, args)
+    # untimed: into the impact (contact established), then the warm-up steps
+    s.step(args.preroll)
     s.step(max(args.warmup, 3))
-    # device-resident timed region: K steps, CUDA events on the solver's stream
+    start_step = s.steps_done()
+    yf0, _ = yield_fraction(s)
     barrier(world)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-        ms = s.time_steps(args.steps)
+        ms, reps = timed_window(s, args, world, 1e3 * args.min_timed_s)
     barrier(world)
-    ms = max_over_ranks(ms, world)
+    end_step = s.steps_done()
+    yf1, ep1 = yield_fraction(s)
     ms_step = ms / args.steps
     value = world * E * args.steps / (ms / 1e3)
     # per-kernel device durations (separate pass, per-launch events)
@@ -277,10 +316,9 @@ def run_ours(args, rank, world):
                  "frac": round(step_bytes / (ms_step * 1e-3) / 1e9 / peak, 4),
                  "bytes_per_elem_step": round(step_bytes / E, 1)}
     # end to end through the C ABI with host buffers: per call, upload the state,
-    # advance S steps, read the state back (an export interval of the reference driver)
+    # advance S steps, read the state back (an export interval of the reference driver);
+    # the state lives in pinned host buffers between calls
     S = args.e2e_interval
-    # the state lives in pinned host buffers between calls (as a driver exporting every
-    # S steps would keep it); each call uploads it, steps and reads it back in place
     try:
         import torch
         xh = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
@@ -288,7 +326,7 @@ def run_ours(args, rank, world):
     except (ImportError, RuntimeError):
         xh, vh = np.empty((N, 3)), np.empty((N, 3))
     s.get_xv(xh, vh)
-    calls = max(1, args.steps // S)
+    calls = max(1, int(np.ceil(args.min_timed_s / (S * ms_step * 1e-3))))
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(calls):
@@ -300,9 +338,11 @@ def run_ours(args, rank, world):
     e2e_s = max_over_ranks(t1 - t0, world)
     e2e = {"value": world * E * S * calls / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": 48 * N / S, "d2h_bytes_per_step": 48 * N / S,
-           "steps_per_call": S,
+           "steps_per_call": S, "calls": calls,
            "api": "per call: ci_set_state(x, v) + ci_step(S) + ci_get_state(x, v), pinned host buffers"}
     en = s.energy()
+    launches = (s.launches_per_step() * args.steps + 1) * len(reps)
+    s.close()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -311,34 +351,70 @@ def run_ours(args, rank, world):
         "config": {"workload": desc, "elements": E, "nodes": N, "nodes_per_element": npe,
                    "dt": setup["dt"], "l2": "working set > L2 (no flush)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "timing": {"repeats": len(reps), "statistic": "median over repeats of K-step windows",
+                   "ms_per_step_min": min(reps) / args.steps,
+                   "ms_per_step_max": max(reps) / args.steps,
+                   "window_steps": [start_step, end_step],
+                   "preroll_steps": args.preroll,
+                   "yielded_qp_frac": [yf0, yf1], "epbar_max_end": ep1},
         "roofline": roofline, "step_roofline": step_roof, "e2e": e2e,
-        "gpu_launches": s.launches_per_step() * args.steps,
+        "gpu_launches": launches,
         "clocks": clk.summary(),
         "energy_balance_rel": abs(en["balance"]) / max(en["kinetic0"], 1e-300),
     }
-    s.close()
+    if args.plastic_speed > 0 and args.workload in ("shell", "shell_half"):
+        line["j2_active"] = run_plastic_window(args, world, m, peak, step_bytes)
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(m, setup, args.cpu_seconds)
-        if args.fp64_check_steps > 0:
-            g = api.Solver(m.xloc, m.conn, **MAT, mode=api.MODE_J2, lumping=api.LUMP_HRZ,
-                           step_kernel=args.step_kernel, chunk_elements=args.chunk_elements,
-                           chunk_nodes=args.chunk_nodes, block_threads=args.block_threads,
-                           elem_lanes=args.elem_lanes, wall_normal=setup["wall_normal"],
-                           wall_offset=setup["wall_offset"],
-                           wall_stiffness=setup["wall_stiffness"],
-                           device=int(os.environ.get("LOCAL_RANK", "0")))
-            g.initialize(setup["vel"])
-            g.start(setup["dt"])
-            g.step(args.fp64_check_steps)
-            line["accuracy"] = fp64_accuracy(m, setup, g.state(("x", "v", "epbar", "contact")),
-                                             args.fp64_check_steps)
-            g.close()
+        line["cpu_baseline"] = cpu_baseline(m, setup)
+    if rank == 0 and args.fp64_check_steps > 0:
+        line["accuracy"] = accuracy_leg(args, m, setup, args.fp64_check_steps)
+        if args.plastic_speed > 0 and args.fp64_check_plastic_steps > 0 and \
+                args.workload in ("shell", "shell_half"):
+            from cppimpact_gb300 import meshgen as mg
+            ps = mg.impact_setup(m, args.plastic_speed, 0.0)
+            line["accuracy_j2_active"] = accuracy_leg(args, m, ps, args.fp64_check_plastic_steps)
     if rank == 0 and args.sweep:
         line["sweep"] = run_sweep(args)
     if rank == 0 and args.sweep and args.surrogate and args.workload == "shell":
-        s.close()
         line["surrogate"] = surrogate_summary()
     return line
+
+
+def run_plastic_window(args, world, m, peak, step_bytes):
+    """The same mesh hitting the plane at --plastic-speed, where the J2 return branch is
+    taken (at the shell's own 5 m/s the peak von Mises stress stays near 0.4 of yield):
+    timed like the headline after --plastic-preroll steps, with the yielded fraction of
+    Gauss points at the start and end of the window."""
+    from cppimpact_gb300 import meshgen as mg
+    setup = mg.impact_setup(m, args.plastic_speed, 0.0)
+    s = make_solver(m, setup, args)
+    s.step(args.plastic_preroll)
+    s.step(max(args.warmup, 3))
+    start_step = s.steps_done()
+    yf0, _ = yield_fraction(s)
+    ms, reps = timed_window(s, args, world, 500.0)
+    yf1, ep1 = yield_fraction(s)
+    end_step = s.steps_done()
+    k_ms, _ = s.time_kernels(min(args.steps, 200))
+    s.close()
+    ms_step = ms / args.steps
+    return {"workload": f"{m.num_elements} tet10 shell, J2, {args.plastic_speed:g} m/s onto the "
+                        "tangent plane",
+            "value": world * m.num_elements * args.steps / (ms / 1e3), "unit": UNIT,
+            "ms_per_step": ms_step, "repeats": len(reps), "window_steps": [start_step, end_step],
+            "yielded_qp_frac": [yf0, yf1], "epbar_max_end": ep1,
+            "kernel_ms": round(k_ms, 4),
+            "roofline_frac": round(step_bytes / (k_ms * 1e-3) / 1e9 / peak, 4)}
+
+
+def accuracy_leg(args, m, setup, nsteps):
+    g = make_solver(m, setup, args)
+    g.step(nsteps)
+    st = g.state(("x", "v", "epbar", "contact"))
+    g.close()
+    out = fp64_accuracy(m, setup, st, nsteps)
+    out["speed"] = float(np.linalg.norm(setup["vel"]))
+    return out
 
 
 def surrogate_summary():
@@ -358,8 +434,11 @@ def surrogate_summary():
             "batched_gpu_runs_per_hour": rph["batched_solver"],
             "peak_disp_err": {"p95": err["p95"], "max": err["max"],
                               "within_2pct": 1.0 - err["frac_over_2pct"]},
-            "reruns": r["audit"]["rerun"], "fit_s": r["fit"]["wall_s"],
+            "reruns": r["audit"]["rerun"], "audit": r["audit"], "fit_s": r["fit"]["wall_s"],
+            "one_off_s": r["one_off_s"], "amortised": r["amortised"],
             "break_even_queries": rph["break_even_queries"],
+            "idw_peak_disp_err": {"p95": r["errors"]["idw_peak_disp"]["p95"],
+                                  "within_2pct": 1.0 - r["errors"]["idw_peak_disp"]["frac_over_2pct"]},
             "gemm_tflops": r["gemm"]["square"]["tflops"]}
 
 
@@ -491,33 +570,33 @@ def run_surrogate(args, rank, world):
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU algorithm (oracle/ref_port.cpp, bitwise identical to the
+    compiled reference on the golden fixtures) with all host threads on the same
+    workload: each step one reference update over a sample of the mesh's elements --
+    the whole mesh when W + K such steps fit the time budget (about two minutes),
+    else the first elements in mesh order."""
     m, setup, desc = workload(args.workload)
     if rank != 0:
         return None
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle_py as op
-    threads = os.cpu_count() or 1
+    op, rp, dof = _ref_setup(m, setup)
+    cores = os.cpu_count() or 1
     E = m.num_elements
-    # bounded sample sized so that each step takes ~0.5 s on this host
-    probe = cpu_baseline(m, setup, seconds_budget=2.0, threads=threads)
-    ne = int(min(E, max(1024, probe["value"] * 0.5)))
+    # probe the per-element rate on a slice, then size the sample
+    ne_probe = min(E, 16384)
+    t = op.ref_time_steps(m.xloc, m.conn[:ne_probe], rp, dof, 1, nthreads=cores)
+    rate = ne_probe / max(t, 1e-9)
+    ne = int(min(E, max(1024, rate * args.reference_budget_s / (args.steps + args.warmup))))
     conn = m.conn[:ne]
     used = np.unique(conn)
     remap = np.full(m.num_nodes, -1, np.int32)
     remap[used] = np.arange(used.size, dtype=np.int32)
     x, c = m.xloc[used], remap[conn]
-    rp = op.ref_params(MAT["E"], MAT["nu"], MAT["rho"], setup["wall_offset"],
-                       setup["wall_stiffness"], 1)
-    dof = np.zeros(3 * used.size)
-    rng = np.random.default_rng(1)
-    dof += rng.normal(scale=1e-7, size=dof.size)
-    for _ in range(max(args.warmup, 0)):
-        op.ref_update(x, c, rp, dof, nthreads=threads)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        op.ref_update(x, c, rp, dof, nthreads=threads)
-    t = time.perf_counter() - t0
+    t = op.ref_time_steps(x, c, rp, dof[:3 * used.size], args.steps, nthreads=cores,
+                          warmup=args.warmup)
     value = ne * args.steps / t
+    sample = (f"{'whole mesh' if ne == E else f'first {ne} of {E} elements'} per step (one "
+              f"reference update: 5-point K_e, gemv, scatter, stress/strain output, wall; mass "
+              f"assembled once), {args.steps} steps after {args.warmup} warm-up")
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
@@ -525,9 +604,8 @@ def run_reference(args, rank, world):
         "data": "synthetic (seeded mesh, seed 20261203)",
         "config": {"workload": desc, "elements": E, "nodes": m.num_nodes,
                    "nodes_per_element": m.npe, "dt": setup["dt"]},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{ne} of {E} elements per step (one reference update: "
-                                   f"5-point K_e, gemv, scatter, wall), {args.steps} steps"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "cores_used": cores,
+                         "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -535,8 +613,9 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10000)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=20,
+                    help="K: steps per timed window (repeated until --min-timed-s)")
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default="shell",
                     choices=["shell", "shell_half", "quad", "small", "surrogate"])
     ap.add_argument("--step-kernel", type=int, default=0, help="0 fused, 1 element + node kernels")
@@ -545,10 +624,23 @@ def main():
     ap.add_argument("--block-threads", type=int, default=0)
     ap.add_argument("--elem-lanes", type=int, default=0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--preroll", type=int, default=2000,
+                    help="untimed steps before the warm-up: the timed windows lie inside the "
+                         "impact (contact established)")
+    ap.add_argument("--min-timed-s", type=float, default=1.0,
+                    help="repeat the K-step window until this much device time is covered")
+    ap.add_argument("--plastic-speed", type=float, default=40.0,
+                    help="shell: also time and check the same mesh at this impact speed, where "
+                         "it yields (0: off)")
+    ap.add_argument("--plastic-preroll", type=int, default=1000)
     ap.add_argument("--e2e-interval", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--fp64-check-steps", type=int, default=20,
+    ap.add_argument("--reference-budget-s", type=float, default=120.0,
+                    help="--impl reference: wall-time budget of its warm-up + timed steps")
+    ap.add_argument("--fp64-check-steps", type=int, default=2000,
                     help="steps of the GPU-vs-FP64 accuracy check on the full mesh (0: off)")
+    ap.add_argument("--fp64-check-plastic-steps", type=int, default=1000,
+                    help="steps of the same check at --plastic-speed (0: off)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep", type=int, default=1, help="also run the 256-instance batched sweep")
     ap.add_argument("--surrogate", type=int, default=1,

@@ -135,6 +135,48 @@ def ref_update(xloc, conn, rp: OrcRefParams, dof, nthreads=1):
     return acc, mass
 
 
+def ref_nodal_fields(xloc0, x, conn, rp: OrcRefParams):
+    """The reference's global_strains / global_stress ([N, 6] each, last element wins)
+    for the state at positions x of a mesh with reference positions xloc0: one update
+    call with a zero increment, so the strain is B(x) (x - xloc0) at xi = 0
+    (include/dynamics_kernels.h:117-147)."""
+    h = _MeshHold(xloc0, conn)
+    n3 = h.x.size
+    acc, mass = np.zeros(n3), np.zeros(n3)
+    xs = np.ascontiguousarray(x, dtype=np.float64).reshape(-1).copy()
+    strains, stress = np.zeros(2 * n3), np.zeros(2 * n3)
+    rc = lib().orc_ref_update(C.byref(h.s), C.byref(rp), _d(h.x), _d(xs), _d(np.zeros(n3)),
+                              _d(acc), _d(mass), _d(strains), _d(stress), 1)
+    assert rc == 0
+    return strains.reshape(-1, 6), stress.reshape(-1, 6)
+
+
+def ref_time_steps(xloc, conn, rp: OrcRefParams, dof, steps, nthreads=1, warmup=0):
+    """Wall time (s) of `steps` calls of the reference's per-step update on the whole
+    mesh -- element loop with the 5-point K_e, gemv, scatter, the stress/strain output
+    the reference computes every step, wall and gravity -- after the lumped mass was
+    assembled once (as Dynamics::solve does: the reference's update skips the mass when
+    global_mass[0] != 0, include/dynamics_kernels.h:36).  `warmup` untimed calls first."""
+    import time
+    h = _MeshHold(xloc, conn)
+    n3 = h.x.size
+    acc, mass = np.zeros(n3), np.zeros(n3)
+    strains, stress = np.zeros(2 * n3), np.zeros(2 * n3)
+    x = h.x.copy()
+    dof = np.ascontiguousarray(dof, dtype=np.float64).reshape(-1)
+    assert lib().orc_ref_lumped_mass(C.byref(h.s), rp.rho, _d(h.x), _d(mass)) == 0
+
+    def one():
+        assert lib().orc_ref_update(C.byref(h.s), C.byref(rp), _d(h.x), _d(x), _d(dof),
+                                    _d(acc), _d(mass), _d(strains), _d(stress), nthreads) == 0
+    for _ in range(warmup):
+        one()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one()
+    return time.perf_counter() - t0
+
+
 def ref_debug_strain(xloc, conn, E, nu, alpha, case):
     h = _MeshHold(xloc, conn)
     W, V = C.c_double(0), C.c_double(0)

@@ -149,8 +149,10 @@ void dmatrix(double E, double nu, double* D) {
   for (int i = 0; i < 36; i++) D[i] *= E / ((1 + nu) * (1 - 2 * nu));
 }
 
-// B^T D B accumulated in the reference's loop order (include/analysis.h:293-319).
-void btdb(int n, const double* B, const double* D, double* out) {
+// B^T D B accumulated in the reference's loop order (include/analysis.h:293-319); n =
+// 3 npe is a compile-time constant there (dof_per_element), and here too.
+template <int n>
+void btdb(const double* B, const double* D, double* out) {
   for (int k = 0; k < 6; ++k) {
     const double* bk = B + k * n;
     for (int l = 0; l < 6; ++l) {
@@ -177,28 +179,36 @@ void gemv(int m, int n, const double* A, const double* x, double* y) {
 // Element stiffness K_e = sum_q w_q detJ_q B^T D B at the given coordinates
 // (calculate_f_internal, include/analysis.h:321-378).  pu_jinv reproduces the
 // Jinv overwrite of calculate_strain_energy.
-void element_stiffness(int npe, const double* xe, const double* D, double* K, bool pu_jinv) {
-  const int n = 3 * npe;
+template <int NPE>
+void element_stiffness_t(const double* xe, const double* D, double* K, bool pu_jinv) {
+  constexpr int n = 3 * NPE;
   std::memset(K, 0, sizeof(double) * n * n);
-  std::vector<double> B(6 * n), T(n * n);
+  double B[6 * n], T[n * n];
   for (int q = 0; q < 5; q++) {
     const double* pt = kQ5Pt[q];
     const double w = kQ5W[q];
     double G[30], J[9], Ji[9];
-    shape_grad(npe, pt, G);
-    jacobian(npe, G, xe, J);
+    shape_grad(NPE, pt, G);
+    jacobian(NPE, G, xe, J);
     const double detJ = inverse3(J, Ji);
-    if (pu_jinv && npe == 10) {
+    if (pu_jinv && NPE == 10) {
       double Gp[30], Jp[9];
       shape_grad_pu(pt, Gp);
-      jacobian(npe, Gp, xe, Jp);
+      jacobian(NPE, Gp, xe, Jp);
       inverse3(Jp, Ji);
     }
-    bmatrix(npe, Ji, G, B.data());
-    std::fill(T.begin(), T.end(), 0.0);
-    btdb(n, B.data(), D, T.data());
+    bmatrix(NPE, Ji, G, B);
+    std::memset(T, 0, sizeof(T));
+    btdb<n>(B, D, T);
     for (int j = 0; j < n * n; j++) K[j] += w * detJ * T[j];
   }
+}
+
+void element_stiffness(int npe, const double* xe, const double* D, double* K, bool pu_jinv) {
+  if (npe == 4)
+    element_stiffness_t<4>(xe, D, K, pu_jinv);
+  else
+    element_stiffness_t<10>(xe, D, K, pu_jinv);
 }
 
 void gather3(int npe, const int* nodes, const double* src, double* dst) {
