@@ -89,6 +89,7 @@ EXPORTS = {
     "ci_get_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _fp, _fp, _ubp]),
     "ci_set_state": (C.c_int, [C.c_void_p, _dp, _dp]),
     "ci_deformation_gradient": (C.c_int, [C.c_void_p, _dp]),
+    "ci_get_nodal_fields": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
     "ci_save_state": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ci_load_state": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ci_get_energy": (C.c_int, [C.c_void_p, C.POINTER(CiEnergy)]),
@@ -284,6 +285,14 @@ class Solver:
         F = np.zeros((self.E, self.nq, 3, 3))
         check(lib().ci_deformation_gradient(self._h, _d(F)))
         return F
+
+    def nodal_fields(self):
+        """The reference's nodal export fields: acceleration [N, 3] of the last step,
+        strain and stress [N, 6] (Voigt xx yy zz gamma_xy gamma_yz gamma_xz; each node
+        takes the value of the last element containing it)."""
+        acc, eps, sig = np.zeros((self.N, 3)), np.zeros((self.N, 6)), np.zeros((self.N, 6))
+        check(lib().ci_get_nodal_fields(self._h, _d(acc), _d(eps), _d(sig)))
+        return {"acc": acc, "strain": eps, "stress": sig}
 
     def set_state(self, x, v):
         x = np.ascontiguousarray(x, dtype=np.float64)

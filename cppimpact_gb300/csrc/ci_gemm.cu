@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -412,9 +413,15 @@ __global__ void k_splitk_reduce(const float* partial, int splits, float* C, int 
   if (Cb) Cb[(size_t)row * ldc + col] = __float2bfloat16(v);
 }
 
-// split-K workspace, grown on demand, one per device
-float* g_ws[64] = {};
-size_t g_ws_size[64] = {};
+// split-K workspaces, grown on demand, one per (device, stream): calls on different
+// streams never share one, so they may run concurrently (the stream orders the calls
+// that do share one)
+struct Workspace {
+  float* p = nullptr;
+  size_t size = 0;
+};
+std::mutex g_ws_mu;
+std::map<std::pair<int, cudaStream_t>, Workspace> g_ws;
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
@@ -542,18 +549,20 @@ extern "C" int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, i
   float* partial = nullptr;
   if (splits > 1) {
     int dev = 0;
-    cudaGetDevice(&dev);
+    if (cudaGetDevice(&dev) != cudaSuccess)
+      return ci::set_last_error(CI_ERR_CUDA, "ci_gemm_bf16: no current device");
     const size_t need = sizeof(float) * (size_t)splits * M * N;
-    if (dev < 0 || dev >= 64) return ci::set_last_error(CI_ERR_CUDA, "ci_gemm_bf16: bad device");
-    if (g_ws_size[dev] < need) {
-      if (g_ws[dev]) cudaFree(g_ws[dev]);
-      g_ws[dev] = nullptr;
-      g_ws_size[dev] = 0;
-      if (cudaMalloc(&g_ws[dev], need) != cudaSuccess)
+    std::lock_guard<std::mutex> lock(g_ws_mu);
+    Workspace& w = g_ws[{dev, st}];
+    if (w.size < need) {
+      if (w.p) cudaFree(w.p);  // synchronises the device: no call still reads it
+      w.p = nullptr;
+      w.size = 0;
+      if (cudaMalloc(&w.p, need) != cudaSuccess)
         return ci::set_last_error(CI_ERR_NOMEM, "ci_gemm_bf16: split-K workspace");
-      g_ws_size[dev] = need;
+      w.size = need;
     }
-    partial = g_ws[dev];
+    partial = w.p;
   }
   dim3 grid((M + BM - 1) / BM, (N + bn - 1) / bn, splits);
   __nv_bfloat16* cb = static_cast<__nv_bfloat16*>(C_bf16);

@@ -617,13 +617,29 @@ __device__ __forceinline__ void complete_node(const FusedArgs& A, const NodePara
   node_step(np, fx, fy, fz, A.mass[g], A.d0f[g], A.d0, g, u, v, a, hit, uf, vf);
 }
 
-// Shared-memory node records of the fused kernels: p0 = (x, y, z, du_x),
-// p1 = (du_y, du_z), acc = (f_x, f_y, f_z, -); 40 bytes per local node.
+// Shared-memory node records of the fused kernels: p0 = (x, du_x, y, du_y),
+// p1 = (z, du_z), acc = (f_x, f_y, f_z, -); 40 bytes per local node.  Each coordinate
+// and its increment are adjacent, so a record loads as three (x_c, du_c) register
+// pairs, the operand shape of the packed FP32 instructions (fma.rn.f32x2).
 struct Tile {
   float4* p0;
   float2* p1;
   float4* acc;
 };
+
+__device__ __forceinline__ void store_record(const Tile& T, int l, float x, float y, float z,
+                                             float dx, float dy, float dz) {
+  T.p0[l] = make_float4(x, dx, y, dy);
+  T.p1[l] = make_float2(z, dz);
+}
+
+// (x_c, du_c) of local node l for c = 0, 1, 2
+__device__ __forceinline__ void load_pairs(const Tile& T, int l, float2 (&p)[3]) {
+  const float4 q0 = T.p0[l];
+  p[0] = make_float2(q0.x, q0.y);
+  p[1] = make_float2(q0.z, q0.w);
+  p[2] = T.p1[l];
+}
 
 __device__ __forceinline__ Tile make_tile(float* sm, int L) {
   Tile t;
@@ -692,8 +708,8 @@ __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams
       node_step(np, f[0], f[1], f[2], m, d0f, A.d0, g, u, v, a, hit, uf, vf);
       if (own) store_node(A, A.u_cur, A.v_cur, g, u, v, vf, a, hit, false, ct);
     }
-    T.p0[l] = make_float4(x0[0] + uf[0], x0[1] + uf[1], x0[2] + uf[2], ep.dt * vf[0]);
-    T.p1[l] = make_float2(ep.dt * vf[1], ep.dt * vf[2]);
+    store_record(T, l, x0[0] + uf[0], x0[1] + uf[1], x0[2] + uf[2], ep.dt * vf[0], ep.dt * vf[1],
+                 ep.dt * vf[2]);
     T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
@@ -762,8 +778,8 @@ __device__ __forceinline__ void stage_nodes_k(const FusedArgs& A, const ElemPara
       node_step(np, f[j][0], f[j][1], f[j][2], m[j], d0f[j], A.d0, g[j], u[j], v[j], a, hit, uf,
                 vf);
       if (l < ch.n_own) store_node(A, A.u_cur, A.v_cur, g[j], u[j], v[j], vf, a, hit, false, ct[j]);
-      T.p0[l] = make_float4(x0[j][0] + uf[0], x0[j][1] + uf[1], x0[j][2] + uf[2], ep.dt * vf[0]);
-      T.p1[l] = make_float2(ep.dt * vf[1], ep.dt * vf[2]);
+      store_record(T, l, x0[j][0] + uf[0], x0[j][1] + uf[1], x0[j][2] + uf[2], ep.dt * vf[0],
+                   ep.dt * vf[1], ep.dt * vf[2]);
       T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
   }
@@ -835,14 +851,13 @@ __global__ void __launch_bounds__(BS) k_step(FusedArgs A, ElemParams ep_arg, Nod
 #pragma unroll
       for (int a = 0; a < NPE; a++) {
         ln[a] = P.conn_local[(size_t)a * E + e];
-        const float4 q0 = T.p0[ln[a]];
-        const float2 q1 = T.p1[ln[a]];
-        x[a][0] = q0.x;
-        x[a][1] = q0.y;
-        x[a][2] = q0.z;
-        du[a][0] = q0.w;
-        du[a][1] = q1.x;
-        du[a][2] = q1.y;
+        float2 pr[3];
+        load_pairs(T, ln[a], pr);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          x[a][c] = pr[c].x;
+          du[a][c] = pr[c].y;
+        }
       }
       element_force<NPE, MODE>(ep, S, e, E, x, du, f, wint, wp, vol);
     }
@@ -926,22 +941,58 @@ __device__ __forceinline__ float tet10_force(const Tet10QP& t, const float* Pa) 
   return fmaf(-t.A3, Pa[0] + Pa[1], (t.A2 - t.A3) * Pa[2]);
 }
 
+// Packed (FP32 pair) form of tet10_grad_acc: c[j] += G_I[j] * (x, du) for one
+// coordinate's (position, increment) pair, two results per instruction
+// (fma.rn.f32x2 / add / mul, sm_100 and later).
+__device__ __forceinline__ float2 bcast(float a) { return make_float2(a, a); }
+
 template <int I>
-__device__ __forceinline__ void tet10_gather(const Tet10QP& t, const Tile& T, int l, float (&J)[9],
-                                             float (&Gu)[9]) {
-  const float4 q0 = T.p0[l];
-  const float2 q1 = T.p1[l];
-  const float xs[3] = {q0.x, q0.y, q0.z}, ds[3] = {q0.w, q1.x, q1.y};
-  float cj[3], cu[3];
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    cj[0] = J[3 * a]; cj[1] = J[3 * a + 1]; cj[2] = J[3 * a + 2];
-    tet10_grad_acc<I>(t, xs[a], cj);
-    J[3 * a] = cj[0]; J[3 * a + 1] = cj[1]; J[3 * a + 2] = cj[2];
-    cu[0] = Gu[3 * a]; cu[1] = Gu[3 * a + 1]; cu[2] = Gu[3 * a + 2];
-    tet10_grad_acc<I>(t, ds[a], cu);
-    Gu[3 * a] = cu[0]; Gu[3 * a + 1] = cu[1]; Gu[3 * a + 2] = cu[2];
+__device__ __forceinline__ void tet10_grad_acc2(const Tet10QP& t, float2 x, float2* c) {
+  if (I == 0) c[0] = __ffma2_rn(bcast(t.A0 - 1.f), x, c[0]);
+  if (I == 1) c[1] = __ffma2_rn(bcast(t.A1 - 1.f), x, c[1]);
+  if (I == 2) {
+    const float2 g = __fmul2_rn(bcast(1.f - t.A2), x);
+    c[0] = __fadd2_rn(c[0], g);
+    c[1] = __fadd2_rn(c[1], g);
+    c[2] = __fadd2_rn(c[2], g);
   }
+  if (I == 3) c[2] = __ffma2_rn(bcast(t.A3 - 1.f), x, c[2]);
+  if (I == 4) {
+    c[0] = __ffma2_rn(bcast(t.A1), x, c[0]);
+    c[1] = __ffma2_rn(bcast(t.A0), x, c[1]);
+  }
+  if (I == 5) {
+    c[0] = __ffma2_rn(bcast(-t.A1), x, c[0]);
+    c[1] = __ffma2_rn(bcast(t.A2 - t.A1), x, c[1]);
+    c[2] = __ffma2_rn(bcast(-t.A1), x, c[2]);
+  }
+  if (I == 6) {
+    c[0] = __ffma2_rn(bcast(t.A2 - t.A0), x, c[0]);
+    c[1] = __ffma2_rn(bcast(-t.A0), x, c[1]);
+    c[2] = __ffma2_rn(bcast(-t.A0), x, c[2]);
+  }
+  if (I == 7) {
+    c[0] = __ffma2_rn(bcast(t.A3), x, c[0]);
+    c[2] = __ffma2_rn(bcast(t.A0), x, c[2]);
+  }
+  if (I == 8) {
+    c[1] = __ffma2_rn(bcast(t.A3), x, c[1]);
+    c[2] = __ffma2_rn(bcast(t.A1), x, c[2]);
+  }
+  if (I == 9) {
+    c[0] = __ffma2_rn(bcast(-t.A3), x, c[0]);
+    c[1] = __ffma2_rn(bcast(-t.A3), x, c[1]);
+    c[2] = __ffma2_rn(bcast(t.A2 - t.A3), x, c[2]);
+  }
+}
+
+// JG[3a + j] = (J, grad du)[a][j] += G_I[j] * (x_a, du_a) for local node l
+template <int I>
+__device__ __forceinline__ void tet10_gather(const Tet10QP& t, const Tile& T, int l, float2 (&JG)[9]) {
+  float2 p[3];
+  load_pairs(T, l, p);
+#pragma unroll
+  for (int a = 0; a < 3; a++) tet10_grad_acc2<I>(t, p[a], &JG[3 * a]);
 }
 
 // Force component c of node I at this lane's point (I < 0: none).
@@ -1006,19 +1057,25 @@ __device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const Ele
       s2 = A.sig_b[qi];
       ep0 = A.epbar[qi];
     }
+    float2 JG[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) JG[k] = make_float2(0.f, 0.f);
+    tet10_gather<0>(t, T, ln[0], JG);
+    tet10_gather<1>(t, T, ln[1], JG);
+    tet10_gather<2>(t, T, ln[2], JG);
+    tet10_gather<3>(t, T, ln[3], JG);
+    tet10_gather<4>(t, T, ln[4], JG);
+    tet10_gather<5>(t, T, ln[5], JG);
+    tet10_gather<6>(t, T, ln[6], JG);
+    tet10_gather<7>(t, T, ln[7], JG);
+    tet10_gather<8>(t, T, ln[8], JG);
+    tet10_gather<9>(t, T, ln[9], JG);
     float J[9], Gu[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) J[k] = Gu[k] = 0.f;
-    tet10_gather<0>(t, T, ln[0], J, Gu);
-    tet10_gather<1>(t, T, ln[1], J, Gu);
-    tet10_gather<2>(t, T, ln[2], J, Gu);
-    tet10_gather<3>(t, T, ln[3], J, Gu);
-    tet10_gather<4>(t, T, ln[4], J, Gu);
-    tet10_gather<5>(t, T, ln[5], J, Gu);
-    tet10_gather<6>(t, T, ln[6], J, Gu);
-    tet10_gather<7>(t, T, ln[7], J, Gu);
-    tet10_gather<8>(t, T, ln[8], J, Gu);
-    tet10_gather<9>(t, T, ln[9], J, Gu);
+    for (int k = 0; k < 9; k++) {
+      J[k] = JG[k].x;
+      Gu[k] = JG[k].y;
+    }
     float Ji[9];
     const float detJ = inv3f(J, Ji);
     if (act && !(detJ > 0.f)) atomicOr(A.status, (unsigned)ST_DEGENERATE);
@@ -1166,19 +1223,19 @@ __device__ __forceinline__ void tet10_bary_element(const ElemParams& ep, const F
   float Yx[4][3], Yd[4][3];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    const float4 q0 = T.p0[ln[k]];
-    const float2 q1 = T.p1[ln[k]];
-    Yx[k][0] = AL * q0.x; Yx[k][1] = AL * q0.y; Yx[k][2] = AL * q0.z;
-    Yd[k][0] = AL * q0.w; Yd[k][1] = AL * q1.x; Yd[k][2] = AL * q1.y;
+    float2 pr[3];
+    load_pairs(T, ln[k], pr);
+    Yx[k][0] = AL * pr[0].x; Yx[k][1] = AL * pr[1].x; Yx[k][2] = AL * pr[2].x;
+    Yd[k][0] = AL * pr[0].y; Yd[k][1] = AL * pr[1].y; Yd[k][2] = AL * pr[2].y;
   }
 #pragma unroll
   for (int k = 0; k < 4; k++)
 #pragma unroll
     for (int l = k + 1; l < 4; l++) {
       const int m = t10_edge(k, l);
-      const float4 q0 = T.p0[ln[m]];
-      const float2 q1 = T.p1[ln[m]];
-      const float xs[3] = {q0.x, q0.y, q0.z}, ds[3] = {q0.w, q1.x, q1.y};
+      float2 pr[3];
+      load_pairs(T, ln[m], pr);
+      const float xs[3] = {pr[0].x, pr[1].x, pr[2].x}, ds[3] = {pr[0].y, pr[1].y, pr[2].y};
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         Yx[k][c] = fmaf(BE, xs[c], Yx[k][c]);
@@ -1200,14 +1257,14 @@ __device__ __forceinline__ void tet10_bary_element(const ElemParams& ep, const F
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       const int m = k == kap ? k : t10_edge(k, kap);
-      const float4 q0 = T.p0[ln[m]];
-      const float2 q1 = T.p1[ln[m]];
-      Cx[k][0] = fmaf(GA, q0.x, Yx[k][0]);
-      Cx[k][1] = fmaf(GA, q0.y, Yx[k][1]);
-      Cx[k][2] = fmaf(GA, q0.z, Yx[k][2]);
-      Cd[k][0] = fmaf(GA, q0.w, Yd[k][0]);
-      Cd[k][1] = fmaf(GA, q1.x, Yd[k][1]);
-      Cd[k][2] = fmaf(GA, q1.y, Yd[k][2]);
+      float2 pr[3];
+      load_pairs(T, ln[m], pr);
+      Cx[k][0] = fmaf(GA, pr[0].x, Yx[k][0]);
+      Cx[k][1] = fmaf(GA, pr[1].x, Yx[k][1]);
+      Cx[k][2] = fmaf(GA, pr[2].x, Yx[k][2]);
+      Cd[k][0] = fmaf(GA, pr[0].y, Yd[k][0]);
+      Cd[k][1] = fmaf(GA, pr[1].y, Yd[k][1]);
+      Cd[k][2] = fmaf(GA, pr[2].y, Yd[k][2]);
     }
     float J[9], Gu[9];
 #pragma unroll

@@ -120,6 +120,9 @@ struct ci_solver {
   DBuf<double> d_Xc, d_xc, d_vc;
   DBuf<int> d_node_new;
   bool xc_stale = true;  // X changed since d_Xc was uploaded
+  // nodal strain/stress output: last element (caller order) of every node, and the plan
+  // position of every caller element (built on first use)
+  std::vector<int> last_elem, elem_new;
 
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
@@ -677,6 +680,65 @@ __global__ void __launch_bounds__(128) k_defgrad(ci::DevPlan P, const double* u0
   }
 }
 
+// Strain and stress output of the reference's update (include/dynamics_kernels.h:117-130,
+// FEAnalysis::calculate_stress_strain, include/analysis.h:479-503), FP64, one thread per
+// element, plan order [E][12]: at the parametric point (0, 0, 0) -- corner 2 of the
+// element geometry, L = (0, 0, 1, 0) -- the Jacobian of the current positions X + u, the
+// strain B u of the total displacement u in the reference's Voigt order (xx, yy, zz,
+// gamma_xy, gamma_yz, gamma_xz; include/tetrahedral.h:442-484) and the stress D strain
+// with the isotropic elastic D of include/tetrahedral.h:486-512.
+template <int NPE>
+__global__ void __launch_bounds__(128) k_elem_strain_stress(ci::DevPlan P, const double* u0,
+                                                            const double* u1, const double* u2,
+                                                            double E, double nu, double* out) {
+  const ci::ChunkInfo ch = P.chunks[blockIdx.x];
+  const double* uk[3] = {u0, u1, u2};
+  // dN/dxi at L = (0, 0, 1, 0): tet4 corners are dL; tet10 corners (4 L_c - 1) dL_c and
+  // edges 4 (L_a dL_b + L_b dL_a), nonzero only on the edges touching corner 2
+  const double dL[4][3] = {{1, 0, 0}, {0, 1, 0}, {-1, -1, -1}, {0, 0, 1}};
+  for (int e = ch.elem_begin + threadIdx.x; e < ch.elem_end; e += blockDim.x) {
+    double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, uu[NPE][3], G[NPE][3];
+    for (int i = 0; i < NPE; i++) {
+      if (NPE == 4) {
+        for (int j = 0; j < 3; j++) G[i][j] = dL[i][j];
+      } else if (i < 4) {
+        for (int j = 0; j < 3; j++) G[i][j] = (i == 2 ? 3.0 : -1.0) * dL[i][j];
+      } else {
+        // edge order 4:(0,1) 5:(1,2) 6:(2,0) 7:(0,3) 8:(1,3) 9:(2,3); L_2 = 1, others 0
+        const int other = i == 5 ? 1 : i == 6 ? 0 : i == 9 ? 3 : -1;
+        for (int j = 0; j < 3; j++) G[i][j] = other < 0 ? 0.0 : 4.0 * dL[other][j];
+      }
+      const int l = P.conn_local[(size_t)i * P.E + e];
+      const int lb = ch.local_begin + l;
+      const int g = l < ch.n_own ? ch.own_begin + l : P.local_gid[lb];
+      for (int k = 0; k < 3; k++) {
+        uu[i][k] = uk[k][g];
+        const double x = (double)P.local_x0[(size_t)k * P.Lt + lb] + uu[i][k];
+        for (int j = 0; j < 3; j++) J[3 * k + j] += x * G[i][j];
+      }
+    }
+    const double c00 = J[4] * J[8] - J[5] * J[7], c01 = J[5] * J[6] - J[3] * J[8],
+                 c02 = J[3] * J[7] - J[4] * J[6];
+    const double r = 1.0 / (J[0] * c00 + J[1] * c01 + J[2] * c02);
+    const double Ji[9] = {c00 * r, (J[2] * J[7] - J[1] * J[8]) * r, (J[1] * J[5] - J[2] * J[4]) * r,
+                          c01 * r, (J[0] * J[8] - J[2] * J[6]) * r, (J[2] * J[3] - J[0] * J[5]) * r,
+                          c02 * r, (J[1] * J[6] - J[0] * J[7]) * r, (J[0] * J[4] - J[1] * J[3]) * r};
+    double L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // L[a][b] = sum_i u_ia dN_i/dx_b
+    for (int i = 0; i < NPE; i++)
+      for (int b = 0; b < 3; b++) {
+        const double dn = Ji[0 * 3 + b] * G[i][0] + Ji[1 * 3 + b] * G[i][1] + Ji[2 * 3 + b] * G[i][2];
+        for (int a = 0; a < 3; a++) L[3 * a + b] += uu[i][a] * dn;
+      }
+    const double eps[6] = {L[0], L[4], L[8], L[1] + L[3], L[5] + L[7], L[2] + L[6]};
+    const double c = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    double* o = out + 12 * (size_t)e;
+    for (int k = 0; k < 6; k++) o[k] = eps[k];
+    for (int k = 0; k < 3; k++)
+      o[6 + k] = c * ((1.0 - nu) * eps[k] + nu * (eps[(k + 1) % 3] + eps[(k + 2) % 3]));
+    for (int k = 3; k < 6; k++) o[6 + k] = c * 0.5 * (1.0 - 2.0 * nu) * eps[k];
+  }
+}
+
 __global__ void k_state_to_caller(const double* u, const double* v, const double* Xc,
                                   const int* node_new, int N, double* xc, double* vc) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -988,6 +1050,66 @@ int ci_deformation_gradient(ci_solver* s, double* F) {
   for (int pe = 0; pe < E; pe++)
     std::memcpy(F + (size_t)9 * nq * P.elem_orig[pe], h.data() + (size_t)9 * nq * pe,
                 sizeof(double) * 9 * nq);
+  return CI_OK;
+}
+
+int ci_get_nodal_fields(ci_solver* s, double* acc, double* strain, double* stress) {
+  if (!s) return fail(CI_ERR_INVALID, "null solver");
+  CI_CUDA(cudaSetDevice(s->device));
+  const int N = s->N, E = s->E;
+  const ci::Plan& P = s->plan;
+  if (acc) {
+    // the last step's acceleration, kept by the step that ends every ci_step call
+    std::vector<float> a(3 * (size_t)N);
+    CI_CUDA(cudaMemcpyAsync(a.data(), s->d_acc.p, sizeof(float) * a.size(), cudaMemcpyDeviceToHost,
+                            s->stream));
+    CI_CUDA(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < N; i++)
+      for (int k = 0; k < 3; k++)
+        acc[3 * (size_t)P.node_orig[i] + k] = (double)a[(size_t)k * N + i];
+  }
+  if (!strain && !stress) return CI_OK;
+  if (s->last_elem.empty()) {
+    // for every node, the last element (caller order) that contains it: the reference
+    // assigns element values to nodes in element order, so that element's value stays
+    s->last_elem.assign(N, -1);
+    for (int c = 0; c < s->C; c++) {
+      const ci::ChunkInfo& ch = P.chunks[c];
+      for (int e = ch.elem_begin; e < ch.elem_end; e++)
+        for (int a = 0; a < s->npe; a++) {
+          const int l = P.conn_local[(size_t)a * E + e];
+          const int g = l < ch.n_own ? ch.own_begin + l : P.local_gid[ch.local_begin + l];
+          int& le = s->last_elem[P.node_orig[g]];
+          le = std::max(le, P.elem_orig[e]);
+        }
+    }
+    s->elem_new.assign(E, 0);
+    for (int e = 0; e < E; e++) s->elem_new[P.elem_orig[e]] = e;
+  }
+  DBuf<double> d;
+  CI_CUDA(d.alloc((size_t)12 * E));
+  const ci::DevPlan dp = s->dev_plan();
+  if (s->npe == 4)
+    k_elem_strain_stress<4><<<s->C, 128, 0, s->stream>>>(dp, s->d_u.p, s->d_u.p + N,
+                                                          s->d_u.p + 2 * (size_t)N, s->mat.E,
+                                                          s->mat.nu, d.p);
+  else
+    k_elem_strain_stress<10><<<s->C, 128, 0, s->stream>>>(dp, s->d_u.p, s->d_u.p + N,
+                                                           s->d_u.p + 2 * (size_t)N, s->mat.E,
+                                                           s->mat.nu, d.p);
+  CI_CUDA(cudaGetLastError());
+  std::vector<double> h((size_t)12 * E);
+  CI_CUDA(cudaMemcpyAsync(h.data(), d.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost,
+                          s->stream));
+  CI_CUDA(cudaStreamSynchronize(s->stream));
+  for (int n = 0; n < N; n++) {
+    const int le = s->last_elem[n];
+    const double* src = le < 0 ? nullptr : h.data() + 12 * (size_t)s->elem_new[le];
+    for (int k = 0; k < 6; k++) {
+      if (strain) strain[6 * (size_t)n + k] = src ? src[k] : 0.0;
+      if (stress) stress[6 * (size_t)n + k] = src ? src[6 + k] : 0.0;
+    }
+  }
   return CI_OK;
 }
 

@@ -5,7 +5,9 @@
 // case), and the public host arrays of the reference (global_xloc, vel, global_mass,
 // global_acc, global_strains, global_stress, vel_i, timestep).  The time loop runs on
 // the GPU inside libcppimpact_gb300.so; the host arrays are filled at each export
-// step and at the end of solve.
+// step and at the end of solve.  The VTK files carry the reference's fields in its
+// order (velocity, strain1/2, stress1/2, acceleration, mass); tet10 cells are written
+// as VTK_QUADRATIC_TETRA (24) where the reference writes VTK_TETRA (10) for both.
 //
 // force_law selects the constitutive model: CI_MODE_REFCOMPAT (default) reproduces the
 // reference's incremental force K_e(x_n) (dt v) with row-sum mass; CI_MODE_J2 uses
@@ -100,18 +102,20 @@ class Dynamics {
     for (double t = 0.0; t <= time_end; t += dt) total++;
     time = 0.0;
     long long done = 0;
-    if (export_interval <= 0) export_interval = INT_MAX;
+    // As in the reference's loop, the step with 0-based index t is exported (after it
+    // ran) when t % export_interval == 0; export_interval <= 0 exports nothing.
     while (done < total) {
-      if (timestep % export_interval == 0) {
-        fetch(dt);
-        export_to_vtk(timestep, vel_i, global_acc, global_mass);
-      }
-      const long long to_next = export_interval - (timestep % export_interval);
-      const int n = (int)std::min<long long>(to_next, total - done);
-      cppimpact_gb300::check(ci_step(solver_, n), "ci_step");
+      long long n = total - done;
+      if (export_interval > 0)
+        n = std::min<long long>(n, (export_interval - timestep % export_interval) % export_interval + 1);
+      cppimpact_gb300::check(ci_step(solver_, (int)n), "ci_step");
       done += n;
-      timestep += n;
+      timestep += (int)n;
       time += n * dt;
+      if (export_interval > 0 && (timestep - 1) % export_interval == 0) {
+        fetch(dt);
+        export_to_vtk(timestep - 1, vel_i, global_acc, global_mass);
+      }
     }
     fetch(dt);
   }
@@ -162,7 +166,17 @@ class Dynamics {
       for (int i = 0; i < mesh->num_nodes; i++)
         f << a[3 * i] << " " << a[3 * i + 1] << " " << a[3 * i + 2] << "\n";
     };
+    // six-component fields as two 3-vectors each (include/dynamics.h:194-225)
+    auto half = [&](const char* name, const T* a, int off) {
+      f << "VECTORS " << name << " double\n";
+      for (int i = 0; i < mesh->num_nodes; i++)
+        f << a[6 * i + off] << " " << a[6 * i + off + 1] << " " << a[6 * i + off + 2] << "\n";
+    };
     vec("velocity", vel_out);
+    half("strain1", global_strains, 0);
+    half("strain2", global_strains, 3);
+    half("stress1", global_stress, 0);
+    half("stress2", global_stress, 3);
     vec("acceleration", acc_out);
     vec("mass", mass_out);
   }
@@ -199,15 +213,19 @@ class Dynamics {
     cppimpact_gb300::check(ci_create(&m, &mat, &w, &o, &solver_), "ci_create");
   }
 
+  // Host arrays from the GPU state: positions, half-step velocity, masses, the last
+  // step's acceleration, the full-step velocity vel - dt/2 acc (include/dynamics.h:501)
+  // and the nodal strain/stress fields (include/dynamics_kernels.h:117-147).
   void fetch(double dt) {
     std::vector<double> m(mesh->num_nodes);
     cppimpact_gb300::check(ci_get_state(solver_, global_xloc, vel, m.data(), nullptr, nullptr, nullptr),
                            "ci_get_state");
+    cppimpact_gb300::check(ci_get_nodal_fields(solver_, global_acc, global_strains, global_stress),
+                           "ci_get_nodal_fields");
     for (int i = 0; i < mesh->num_nodes; i++)
       for (int k = 0; k < 3; k++) {
         global_mass[3 * i + k] = m[i];
-        vel_i[3 * i + k] = vel[3 * i + k];
+        vel_i[3 * i + k] = vel[3 * i + k] - 0.5 * dt * global_acc[3 * i + k];
       }
-    (void)dt;
   }
 };

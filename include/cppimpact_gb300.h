@@ -159,6 +159,17 @@ int ci_set_state(ci_solver* s, const double* x, const double* v);
  * include/dynamics_kernels.h:75-139); this is the reported output of the new
  * deformation-gradient row. */
 int ci_deformation_gradient(ci_solver* s, double* F);
+/* Nodal output fields of the reference's VTK export (include/dynamics.h:113-254), in the
+ * caller's node order; any pointer may be NULL.  acc [3N]: the acceleration of the last
+ * completed step (the reference's global_acc).  strain, stress [6N]: the reference's
+ * global_strains / global_stress (include/dynamics_kernels.h:117-147): for each element
+ * the strain B u of the total displacement u = x - X at the parametric point (0, 0, 0)
+ * with B from the current positions, Voigt order xx yy zz gamma_xy gamma_yz gamma_xz,
+ * and the elastic stress D strain (include/analysis.h:479-503, tetrahedral.h:442-512);
+ * every node takes the value of the last element, in the caller's element order, that
+ * contains it.  Computed on the GPU in FP64 on demand (an export-time field, not part
+ * of the step). */
+int ci_get_nodal_fields(ci_solver* s, double* acc, double* strain, double* stress);
 /* Binary state file of a started solver -- the state the reference's export_to_vtk
  * dumps (include/dynamics.h:113-254) plus everything a restart needs: positions,
  * velocities, masses, contact history, stored stress and plastic strain at the Gauss
@@ -243,9 +254,9 @@ int ci_batch_run_peaks(ci_batch* b, int every, int max_snaps, float* peak_disp, 
  * BF16 copy.  All pointers are device pointers.  *d_error (device int) is set to 1 if
  * a tensor-core wait timed out (the result is then invalid).  When the output has few
  * 128-row tiles and K is long, K is split across CTAs: partial tiles go to a per-device
- * FP32 workspace (grown by cudaMalloc on first need) and are summed in a fixed order, so
- * results are deterministic; concurrent calls on different streams of one device must
- * not overlap.  Three paths, all with the same epilogue (alpha, beta C, bias, tanh,
+ * FP32 workspace (one per device and stream, grown by cudaMalloc on first need) and are
+ * summed in a fixed order, so results are deterministic; calls on different streams may
+ * run concurrently.  Three paths, all with the same epilogue (alpha, beta C, bias, tanh,
  * BF16 copy): C = A B^T with both operands K-major (transA = 0, transB = 1), M >= 128,
  * N >= 16, K >= 64, 16-byte aligned A and B and leading dimensions that are multiples
  * of 8 runs on a TMA-fed pipelined tensor-core kernel; any other form with at most

@@ -337,3 +337,26 @@ def test_deformation_gradient(cilib, order, n):
         Fr[:, q] = np.eye(3) + Gu @ np.linalg.inv(J0)
     assert np.abs(Fr - np.eye(3)).max() > 1e-3, "the case must deform"
     assert rel(F - np.eye(3), Fr - np.eye(3)) < 1e-5
+
+
+@pytest.mark.parametrize("order,n", [(1, 4), (2, 3)])
+def test_nodal_fields_match_reference_output(cilib, oracle, order, n):
+    """ci_get_nodal_fields: the reference's global_strains / global_stress for the current
+    state (strain B u at xi = 0 from the current positions, elastic D, last element in
+    caller order wins per node; include/dynamics_kernels.h:117-147) against the restated
+    reference fed the same positions, and the stored acceleration against the change of
+    the half-step velocity over one step (v_{n+1/2} - v_{n-1/2} = dt a_n)."""
+    m = mg.cube(n, order)
+    setup = mg.impact_setup(m, 20.0, 1e-4)
+    s = _run_gpu(cilib, m, setup, cilib.MODE_J2, 150)
+    v_prev = s.state(("v",))["v"]
+    s.step(1)
+    st = s.state(("x", "v"))
+    fld = s.nodal_fields()
+    rp = oracle.ref_params(E, NU, RHO, setup["wall_offset"], setup["wall_stiffness"], 1)
+    eps_ref, sig_ref = oracle.ref_nodal_fields(m.xloc, st["x"], m.conn, rp)
+    assert np.abs(eps_ref).max() > 1e-5  # the impact strains the cube
+    assert rel(fld["strain"], eps_ref) < 1e-5
+    assert rel(fld["stress"], sig_ref) < 1e-5
+    acc_fd = (st["v"] - v_prev) / setup["dt"]
+    assert rel(fld["acc"], acc_fd) < 1e-5

@@ -140,7 +140,54 @@ def test_small_study_audit_and_fallback(cilib):
     a = r["audit"]
     assert a["audited"] == 4 or a["audited"] == 40 - a["flagged_by_spread"]
     assert a["rerun"] == a["flagged_by_spread"] + a["audited"]
+    am = {row["queries"]: row for row in r["amortised"]}
+    assert am[40]["runs_per_hour"] < am[1_000_000]["runs_per_hour"]
     assert r["errors"]["final_peak_disp"]["max"] <= r["errors"]["surrogate_only_peak_disp"]["max"] + 1e-12
     rph = r["runs_per_hour"]
     assert rph["surrogate"] > 0 and rph["plain_gpu_solver"] > 0 and rph["batched_solver"] > 0
     assert r["gemm"]["pod"]["tflops"] > 0 and r["gemm"]["square"]["tflops"] > 0
+
+
+def test_network_beats_the_method_without_it(cilib):
+    """What the trained network gains: on held-out parameter sets its peak-displacement
+    error is well below that of the same pipeline without the network (inverse-distance
+    interpolation of the training runs' modal trajectories, Surrogate.predict_idw)."""
+    pytest.importorskip("torch")
+    from cppimpact_gb300 import surrogate as sg
+    cfg = sg.Config(n_cube=6, steps=800, every=50, rank=16, hidden=128, n_train=512,
+                    n_test=128, epochs=400, batch=64, ensemble=2)
+    rng = np.random.default_rng(cfg.seed)
+    ptr, pte = sg.sample_params(cfg.n_train, rng), sg.sample_params(cfg.n_test, rng)
+    s_tr, ep_tr, _ = sg.generate(ptr, cfg)
+    s_te, _, _ = sg.generate(pte, cfg)
+    truth = sg.peak_disp(s_te).cpu().numpy()
+    sur = sg.Surrogate(cfg)
+    sur.fit(ptr, s_tr, ep_tr)
+    mean, _ = sur.predict(pte)
+    idw, _ = sur.predict_idw(pte)
+    e_net = np.abs(mean.cpu().numpy() - truth) / truth
+    e_idw = np.abs(idw.cpu().numpy() - truth) / truth
+    assert np.median(e_net) < 0.5 * np.median(e_idw)
+    assert np.quantile(e_net, 0.95) < np.quantile(e_idw, 0.95)
+
+
+def test_concurrent_member_training_is_bitwise_sequential(cilib):
+    """Ensemble members trained at the same time on their own streams (as Surrogate.fit
+    does) end with the same parameters as members trained one after the other; the
+    split-K products of their backward pass use per-stream workspaces."""
+    torch = pytest.importorskip("torch")
+    from cppimpact_gb300 import surrogate as sg
+    rng = np.random.default_rng(7)
+    X = torch.tensor(rng.uniform(-1, 1, (1024, 4)).astype(np.float32), device="cuda")
+    T = torch.tensor(0.3 * rng.standard_normal((1024, 1280)).astype(np.float32), device="cuda")
+    cfg = sg.Config(epochs=12, batch=256)
+    sur = sg.Surrogate.__new__(sg.Surrogate)
+    sur.cfg = cfg
+    seq = [sg.MLP(4, 256, 1280, 11 + j) for j in range(3)]
+    for j, net in enumerate(seq):
+        sur._train(net, X, T, 5 + j)
+    par = [sg.MLP(4, 256, 1280, 11 + j) for j in range(3)]
+    sur._train_concurrently([(net, X, T, 5 + j) for j, net in enumerate(par)])
+    torch.cuda.synchronize()
+    for a, b in zip(seq, par):
+        assert np.array_equal(a.params(), b.params())
