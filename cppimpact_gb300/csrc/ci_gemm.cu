@@ -23,7 +23,10 @@
 // rows takes a pipelined kernel instead: TMA (cp.async.bulk.tensor, 128-byte swizzle)
 // streams 128 x 64 and BN x 64 tiles through a 4-stage shared-memory ring, one thread
 // issues the TMA loads, one thread the MMAs, and mbarriers hand stages back and forth
-// (full: TMA bytes landed; empty: the MMAs reading a stage completed).
+// (full: TMA bytes landed; empty: the MMAs reading a stage completed).  Without split-K
+// that kernel is persistent (k_gemm_tma_pers: one CTA per SM walking the tiles, two
+// TMEM accumulators so the epilogue of one tile overlaps the MMAs of the next); with
+// split-K (few output tiles, long K) it runs one CTA per (tile, K range).
 #include <cuda.h>  // CUtensorMap and its enums; the encoder is fetched at run time
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -396,6 +399,240 @@ __global__ void __launch_bounds__(128, 1)
                  : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Persistent form of the A B^T kernel: one CTA per SM walks the output tiles (grouped
+// raster: GM consecutive 128-row tiles share every BN-column tile, so the operand
+// panels in flight stay in L2).  Six warps with fixed roles:
+//   warp 0  TMA producer: 128 x 64 and BN x 64 tiles into a TSTAGES-deep ring;
+//   warp 1  MMA issuer: tcgen05.mma into one of two TMEM accumulators (2 x BN columns),
+//           tcgen05.commit releases ring stages and, after a tile's last K step,
+//           hands the accumulator to the epilogue;
+//   warps 2-5  epilogue: TMEM lane quarter (warp % 4), tcgen05.ld, alpha / beta / bias /
+//           tanh, stores; then the accumulator goes back to the MMA issuer.
+// The epilogue of tile i overlaps the MMAs of tile i + 1.  Every wait is bounded; a role
+// that times out raises a shared abort flag so the others stop waiting, and the kernel
+// reports the error through *err.
+constexpr int PERS_THREADS = 192;
+constexpr int GROUP_M = 16;
+
+__device__ __forceinline__ bool mbar_wait_abort(uint32_t bar, uint32_t phase, volatile int* abort) {
+  for (unsigned it = 0; it < kSpinLimit; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (done) return true;
+    if ((it & 255u) == 255u && *abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+
+__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int& mt, int& nt) {
+  const int per_group = GROUP_M * tiles_n;
+  const int g = t / per_group;
+  const int m_base = g * GROUP_M;
+  const int gm = min(GROUP_M, tiles_m - m_base);
+  const int r = t - g * per_group;
+  mt = m_base + r % gm;
+  nt = r / gm;
+}
+
+template <int BN>
+__global__ void __launch_bounds__(PERS_THREADS, 1)
+    k_gemm_tma_pers(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                    float* C, int ldc, __nv_bfloat16* Cb, int M, int N, int K, float alpha,
+                    float beta, const float* __restrict__ bias, int act, int* err) {
+  constexpr int A_BYTES = BM * TBK * 2;
+  constexpr int B_BYTES = BN * TBK * 2;
+  constexpr uint32_t TCOLS = 2 * BN;  // two accumulators of BN FP32 columns
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + TSTAGES * A_BYTES;
+  __shared__ __align__(8) uint64_t full[TSTAGES], empty[TSTAGES], tfull[2], tempty[2];
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
+  const int tiles = tiles_m * tiles_n;
+  const int ktiles = (K + TBK - 1) / TBK;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < TSTAGES; s++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&full[s])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&empty[s])) : "memory");
+    }
+    for (int b = 0; b < 2; b++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&tfull[b])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(smem_u32(&tempty[b])) : "memory");
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  volatile int* abort = &abort_flag;
+  bool ok = true;
+  long long issued = 0;  // producer: ring steps whose loads were issued
+  if (warp == 0) {
+    if (lane == 0) {
+      long long it = 0;
+      for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+        int mt, nt;
+        tile_coords(t, tiles_m, tiles_n, mt, nt);
+        for (int kt = 0; kt < ktiles; kt++, it++) {
+          const int s = (int)(it % TSTAGES);
+          if (it >= TSTAGES &&
+              !mbar_wait_abort(smem_u32(&empty[s]), (uint32_t)((it / TSTAGES) - 1) & 1u, abort)) {
+            ok = false;
+            break;
+          }
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
+                           smem_u32(&full[s])),
+                       "r"(A_BYTES + B_BYTES)
+                       : "memory");
+          tma_load_2d(smem_u32(sA + s * A_BYTES), &tmA, kt * TBK, mt * BM, smem_u32(&full[s]));
+          tma_load_2d(smem_u32(sB + s * B_BYTES), &tmB, kt * TBK, nt * BN, smem_u32(&full[s]));
+          issued = it + 1;
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = instr_desc(BM, BN);
+      long long it = 0;
+      int j = 0;
+      for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, j++) {
+        const int b = j & 1;
+        if (j >= 2 && !mbar_wait_abort(smem_u32(&tempty[b]), (uint32_t)((j >> 1) - 1) & 1u, abort)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t acc_tmem = tmem + (uint32_t)(b * BN);
+        for (int kt = 0; kt < ktiles; kt++, it++) {
+          const int s = (int)(it % TSTAGES);
+          if (!mbar_wait_abort(smem_u32(&full[s]), (uint32_t)(it / TSTAGES) & 1u, abort)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+          for (int kk = 0; kk < TBK / 16; kk++) {
+            const uint64_t da = desc_sw128(smem_u32(sA + s * A_BYTES) + kk * 32);
+            const uint64_t db = desc_sw128(smem_u32(sB + s * B_BYTES) + kk * 32);
+            const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc_tmem),
+                "l"(da), "l"(db), "r"(idesc), "r"(acc)
+                : "memory");
+          }
+          asm volatile(
+              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                  smem_u32(&empty[s]))
+              : "memory");
+        }
+        if (!ok) break;
+        // the accumulator is complete once every MMA issued so far has finished
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                smem_u32(&tfull[b]))
+            : "memory");
+      }
+    }
+  } else {
+    const int q = warp & 3;  // TMEM lanes 32 q .. 32 q + 31 (a warp's accessible quarter)
+    int j = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x, j++) {
+      const int b = j & 1;
+      if (!mbar_wait_abort(smem_u32(&tfull[b]), (uint32_t)(j >> 1) & 1u, abort)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      int mt, nt;
+      tile_coords(t, tiles_m, tiles_n, mt, nt);
+      const int row = mt * BM + q * 32 + lane;
+      const int n0 = nt * BN;
+#pragma unroll 1
+      for (int c = 0; c < BN; c += 16) {
+        uint32_t r[16];
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + c);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+            "%11, %12, %13, %14, %15}, [%16];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+              "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+              "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (row < M) {
+          float v[16];
+#pragma unroll
+          for (int jj = 0; jj < 16; jj++) {
+            const int col = n0 + c + jj;
+            v[jj] = alpha * __uint_as_float(r[jj]);
+            if (col < N) {
+              if (beta != 0.f) v[jj] += beta * C[(size_t)row * ldc + col];
+              if (bias) v[jj] += bias[col];
+              if (act == 1) v[jj] = tanhf(v[jj]);
+            }
+          }
+          float* crow = C + (size_t)row * ldc + n0 + c;
+          if (n0 + c + 16 <= N && (reinterpret_cast<uintptr_t>(crow) & 15) == 0) {
+#pragma unroll
+            for (int k4 = 0; k4 < 4; k4++)
+              reinterpret_cast<float4*>(crow)[k4] =
+                  make_float4(v[4 * k4], v[4 * k4 + 1], v[4 * k4 + 2], v[4 * k4 + 3]);
+          } else {
+#pragma unroll
+            for (int jj = 0; jj < 16; jj++)
+              if (n0 + c + jj < N) crow[jj] = v[jj];
+          }
+          if (Cb)
+#pragma unroll
+            for (int jj = 0; jj < 16; jj++)
+              if (n0 + c + jj < N) Cb[(size_t)row * ldc + n0 + c + jj] = __float2bfloat16(v[jj]);
+        }
+      }
+      // this warp's quarter of the accumulator is read: hand it back to the MMA issuer
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      __syncwarp();
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(&tempty[b]))
+                     : "memory");
+    }
+  }
+  ok = __syncthreads_and(ok) != 0;
+  if (!ok) {
+    // let the TMA loads still in flight land before the shared memory goes away
+    if (warp == 0 && lane == 0)
+      for (long long it = issued > TSTAGES ? issued - TSTAGES : 0; it < issued; it++)
+        mbar_wait(smem_u32(&full[it % TSTAGES]), (uint32_t)(it / TSTAGES) & 1u);
+    if (tid == 0) atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS)
+                 : "memory");
+}
+
 // C = alpha sum_z partial[z] (z in order) + beta C + bias, then tanh; BF16 copy.
 __global__ void k_splitk_reduce(const float* partial, int splits, float* C, int ldc,
                                 __nv_bfloat16* Cb, int M, int N, float alpha, float beta,
@@ -477,6 +714,35 @@ cudaError_t launch_tma(const CUtensorMap& ta, const CUtensorMap& tb, dim3 grid, 
   }
   k_gemm_tma<BN><<<grid, 128, tma_smem_bytes<BN>(), st>>>(ta, tb, C, ldc, Cb, M, N, K, alpha, beta,
                                                          bias, act, err, k_chunk, partial);
+  return cudaGetLastError();
+}
+
+int num_sms() {
+  static int n[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 1;
+  if (!n[dev]) cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev);
+  return n[dev] > 0 ? n[dev] : 1;
+}
+
+template <int BN>
+cudaError_t launch_tma_pers(const CUtensorMap& ta, const CUtensorMap& tb, cudaStream_t st, float* C,
+                            int ldc, __nv_bfloat16* Cb, int M, int N, int K, float alpha,
+                            float beta, const float* bias, int act, int* err) {
+  static bool configured[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !configured[dev]) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        k_gemm_tma_pers<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, tma_smem_bytes<BN>());
+    if (e != cudaSuccess) return e;
+    configured[dev] = true;
+  }
+  const int tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+  const int grid = std::min(tiles, num_sms());
+  k_gemm_tma_pers<BN><<<grid, PERS_THREADS, tma_smem_bytes<BN>(), st>>>(
+      ta, tb, C, ldc, Cb, M, N, K, alpha, beta, bias, act, err);
   return cudaGetLastError();
 }
 
@@ -567,7 +833,15 @@ extern "C" int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, i
   dim3 grid((M + BM - 1) / BM, (N + bn - 1) / bn, splits);
   __nv_bfloat16* cb = static_cast<__nv_bfloat16*>(C_bf16);
   cudaError_t le = cudaSuccess;
-  if (tma) {
+  if (tma && splits == 1) {
+    if (bn == 64)
+      le = launch_tma_pers<64>(ta, tb, st, C, ldc, cb, M, N, K, alpha, beta, bias, activation, d_error);
+    else if (bn == 128)
+      le = launch_tma_pers<128>(ta, tb, st, C, ldc, cb, M, N, K, alpha, beta, bias, activation, d_error);
+    else
+      le = launch_tma_pers<256>(ta, tb, st, C, ldc, cb, M, N, K, alpha, beta, bias, activation, d_error);
+    if (le != cudaSuccess) return ci::set_last_error(CI_ERR_CUDA, cudaGetErrorString(le));
+  } else if (tma) {
     if (bn == 64)
       le = launch_tma<64>(ta, tb, grid, st, C, ldc, cb, M, N, K, alpha, beta, bias, activation,
                           d_error, k_chunk, partial);

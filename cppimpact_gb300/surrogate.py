@@ -598,13 +598,31 @@ def time_training(n_in=4, hidden=256, n_out=5120, rows=4096, batch=256, epochs=2
     return ms
 
 
+def time_square_gemm(n: int, reps: int = 10) -> dict:
+    """TFLOP/s of C = A B^T for n x n BF16 operands (K-major, the persistent TMA kernel),
+    best of three timings of `reps` back-to-back calls."""
+    torch = _torch()
+    A = torch.randn((n, n), device="cuda").to(torch.bfloat16)
+    B = torch.randn((n, n), device="cuda").to(torch.bfloat16)
+    out = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    ms = min(_time_gemm(A, B, out, reps) for _ in range(3))
+    return dict(n=n, ms=ms, tflops=2.0 * n ** 3 / (ms * 1e-3) / 1e12)
+
+
 if __name__ == "__main__":
     import argparse
 
-    ap = argparse.ArgumentParser(description="time one surrogate MLP member's training")
+    ap = argparse.ArgumentParser(description="time one surrogate MLP member's training, or "
+                                             "(--gemm N) the square BF16 GEMM")
     ap.add_argument("--hidden", type=int, default=256)
     ap.add_argument("--n-out", type=int, default=5120)
     ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--gemm", type=int, default=0, help="time an N x N x N A B^T instead")
+    ap.add_argument("--reps", type=int, default=10)
     a = ap.parse_args()
-    print(f"{a.epochs} epochs, 4 -> {a.hidden} -> {a.hidden} -> {a.n_out}: "
-          f"{time_training(hidden=a.hidden, n_out=a.n_out, epochs=a.epochs):.2f} ms/epoch")
+    if a.gemm:
+        r = time_square_gemm(a.gemm, a.reps)
+        print(f"{r['n']}^3 BF16 A B^T: {r['ms']:.3f} ms, {r['tflops']:.1f} TFLOP/s")
+    else:
+        print(f"{a.epochs} epochs, 4 -> {a.hidden} -> {a.hidden} -> {a.n_out}: "
+              f"{time_training(hidden=a.hidden, n_out=a.n_out, epochs=a.epochs):.2f} ms/epoch")

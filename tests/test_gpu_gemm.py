@@ -121,3 +121,21 @@ def test_gemm_bf16_nt_pipelined(cilib, M, N, K):
     assert np.array_equal(c, c2)
     c3, ref3, _ = _gemm(cilib, torch, A * 0.1, B * 0.1, 0, 1, act=1, beta=0.5, C0=rng.standard_normal((M, N)))
     assert np.abs(c3 - ref3).max() < 5e-3
+
+
+@pytest.mark.parametrize("M,N,K,act", [(4173, 1100, 160, 0), (16389, 640, 128, 1), (300, 2000, 1000, 0)])
+def test_gemm_tma_persistent_many_tiles(cilib, M, N, K, act):
+    """A B^T with K-major operands on the persistent kernel: more output tiles than SMs
+    (each CTA walks several tiles through the two TMEM accumulators), ragged M, N and K,
+    beta C, bias and tanh in the epilogue; two calls give identical bits."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(M + N + K)
+    A = rng.standard_normal((M, K)) * 0.3
+    B = rng.standard_normal((N, K)) * 0.3
+    bias = rng.standard_normal(N) * 0.1
+    C0 = rng.standard_normal((M, N))
+    c, ref, cb = _gemm(cilib, torch, A, B, 0, 1, bias=bias, act=act, beta=0.5, C0=C0)
+    assert np.linalg.norm(c - ref) <= 1e-3 * np.linalg.norm(ref)
+    assert np.all(np.abs(cb - c) <= 2.0 ** -8 * np.abs(c))
+    c2, _, _ = _gemm(cilib, torch, A, B, 0, 1, bias=bias, act=act, beta=0.5, C0=C0)
+    assert np.array_equal(c, c2)
