@@ -78,7 +78,7 @@ def workload(name: str):
 # DRAM bytes (read + write) per launch of the step kernel, from the ncu capture
 # summarised in profiles/k_step_qp10_shell_half.md (half shell, scaled x2 for the full
 # shell: elements and nodes double exactly).
-MEASURED_TRAFFIC = {"shell": 2 * 118.28e6, "shell_half": 118.28e6}
+MEASURED_TRAFFIC = {"shell": 2 * 117.89e6, "shell_half": 117.89e6}
 
 
 def algorithmic_bytes(npe: int, E: int, N: int):
