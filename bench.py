@@ -234,6 +234,7 @@ def fp64_accuracy(m, setup, gpu, nsteps):
             "yielded_qp_frac": float((ref["epbar"] > 0).mean()),
             "contact_nodes": int(ever_ref.sum()),
             "contact_sets_equal": bool(np.array_equal(ever, ever_ref)),
+            "contact_nodes_differing": int((ever != ever_ref).sum()),
             "fp64_seconds": round(t, 1)}
 
 
