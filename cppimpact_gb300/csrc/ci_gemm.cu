@@ -652,11 +652,15 @@ __global__ void k_splitk_reduce(const float* partial, int splits, float* C, int 
 
 // split-K workspaces, grown on demand, one per (device, stream): calls on different
 // streams never share one, so they may run concurrently (the stream orders the calls
-// that do share one)
+// that do share one).  At most kMaxWorkspaces are kept per device; a new stream beyond
+// that frees the device's others first.  A caller holds g_ws_mu from the lookup until
+// its kernels are enqueued, and cudaFree synchronises the device, so no workspace is
+// freed while a call still uses it.
 struct Workspace {
   float* p = nullptr;
   size_t size = 0;
 };
+constexpr size_t kMaxWorkspaces = 32;
 std::mutex g_ws_mu;
 std::map<std::pair<int, cudaStream_t>, Workspace> g_ws;
 
@@ -813,12 +817,26 @@ extern "C" int ci_gemm_bf16(const void* A, int lda, int transA, const void* B, i
   k_chunk = (k_chunk + BK - 1) / BK * BK;
   splits = (K + k_chunk - 1) / k_chunk;
   float* partial = nullptr;
+  std::unique_lock<std::mutex> ws_lock(g_ws_mu, std::defer_lock);  // held until enqueued
   if (splits > 1) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess)
       return ci::set_last_error(CI_ERR_CUDA, "ci_gemm_bf16: no current device");
     const size_t need = sizeof(float) * (size_t)splits * M * N;
-    std::lock_guard<std::mutex> lock(g_ws_mu);
+    ws_lock.lock();
+    if (!g_ws.count({dev, st})) {
+      size_t on_dev = 0;
+      for (const auto& kv : g_ws) on_dev += kv.first.first == dev;
+      if (on_dev >= kMaxWorkspaces)
+        for (auto it = g_ws.begin(); it != g_ws.end();) {
+          if (it->first.first == dev) {
+            if (it->second.p) cudaFree(it->second.p);
+            it = g_ws.erase(it);
+          } else {
+            ++it;
+          }
+        }
+    }
     Workspace& w = g_ws[{dev, st}];
     if (w.size < need) {
       if (w.p) cudaFree(w.p);  // synchronises the device: no call still reads it

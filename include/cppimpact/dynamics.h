@@ -105,7 +105,7 @@ class Dynamics {
     // As in the reference's loop, the step with 0-based index t is exported (after it
     // ran) when t % export_interval == 0; export_interval <= 0 exports nothing.
     while (done < total) {
-      long long n = total - done;
+      long long n = std::min<long long>(total - done, INT_MAX);
       if (export_interval > 0)
         n = std::min<long long>(n, (export_interval - timestep % export_interval) % export_interval + 1);
       cppimpact_gb300::check(ci_step(solver_, (int)n), "ci_step");

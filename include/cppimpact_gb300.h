@@ -254,9 +254,9 @@ int ci_batch_run_peaks(ci_batch* b, int every, int max_snaps, float* peak_disp, 
  * BF16 copy.  All pointers are device pointers.  *d_error (device int) is set to 1 if
  * a tensor-core wait timed out (the result is then invalid).  When the output has few
  * 128-row tiles and K is long, K is split across CTAs: partial tiles go to a per-device
- * FP32 workspace (one per device and stream, grown by cudaMalloc on first need) and are
- * summed in a fixed order, so results are deterministic; calls on different streams may
- * run concurrently.  Three paths, all with the same epilogue (alpha, beta C, bias, tanh,
+ * FP32 workspace (one per device and stream, grown by cudaMalloc on first need, at most
+ * 32 streams' kept per device) and are summed in a fixed order, so results are
+ * deterministic; calls on different streams may run concurrently.  Three paths, all with the same epilogue (alpha, beta C, bias, tanh,
  * BF16 copy): C = A B^T with both operands K-major (transA = 0, transB = 1), M >= 128,
  * N >= 16, K >= 64, 16-byte aligned A and B and leading dimensions that are multiples
  * of 8 runs on a TMA-fed pipelined tensor-core kernel; any other form with at most

@@ -139,3 +139,23 @@ def test_gemm_tma_persistent_many_tiles(cilib, M, N, K, act):
     assert np.all(np.abs(cb - c) <= 2.0 ** -8 * np.abs(c))
     c2, _, _ = _gemm(cilib, torch, A, B, 0, 1, bias=bias, act=act, beta=0.5, C0=C0)
     assert np.array_equal(c, c2)
+
+
+def test_gemm_split_k_on_many_streams(cilib):
+    """Split-K products on 40 streams in turn (more than the 32 workspaces kept per
+    device, so older streams' workspaces are freed and rebuilt) all give the result of
+    a single-stream call, bit for bit."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(17)
+    A = rng.standard_normal((64, 20000))
+    B = rng.standard_normal((20000, 64))
+    ref, _, _ = _gemm(cilib, torch, A, B, 0, 0)
+    # torch hands out streams from pools of 32 per priority: 20 of each of two
+    # priorities are 40 distinct streams
+    streams = [torch.cuda.Stream(priority=p) for p in (0, -1) for _ in range(20)]
+    assert len({st.cuda_stream for st in streams}) == 40
+    for _ in range(2):
+        for st in streams:
+            with torch.cuda.stream(st):
+                c, _, _ = _gemm(cilib, torch, A, B, 0, 0)
+            assert np.array_equal(c, ref)
