@@ -133,3 +133,77 @@ def test_gemv_keeps_reference_semantics(tmp_path):
                    1 + 0.25 - (0.5 + 12), 2 + 0.25 - (1 + 15), 3 + 0.25 - (1.5 + 18)]
     if os.path.isfile(os.path.join(REF, "include", "cppimpact_blas.h")):
         assert got == _run_gemv(tmp_path, "ref", os.path.join(REF, "include"))
+
+
+DRIVER_J2 = r'''
+#include <cstdio>
+#include "include/analysis.h"
+#include "include/elastoplastic.h"
+#include "include/wall.h"
+#include "include/dynamics.h"
+int main(int argc, char** argv) {
+  Mesh<T, Basis::nodes_per_element> mesh;
+  if (mesh.load_mesh(argv[1]) != 0) return 1;
+  // a low yield stress so the impact yields: the drop-in's J2 law reads Y0 and H
+  Elastoplastic<T, 3> material(68.9e9, 2700, 0.33, 0.0, 0.689e9, 60e6, "AL-soft");
+  Wall<T, 2, Basis> w("Wall", atof(argv[2]), atof(argv[3]), mesh.slave_nodes, mesh.num_slave_nodes, 1);
+  Dynamics<T, Basis, Analysis, Quadrature> dyna(&mesh, &material, &w);
+  dyna.force_law = CI_MODE_J2;
+  dyna.output_dir = argv[5];
+  T pos[] = {0, 0, 0}, vel[] = {0, 0, -20};
+  dyna.initialize(pos, vel);
+  const double dt = atof(argv[4]);
+  dyna.solve(dt, 299 * dt + 0.5 * dt, 150);
+  FILE* f = fopen(argv[6], "wb");
+  fwrite(dyna.global_xloc, sizeof(double), dyna.ndof, f);
+  fwrite(dyna.vel, sizeof(double), dyna.ndof, f);
+  fwrite(dyna.global_strains, sizeof(double), 2 * dyna.ndof, f);
+  fwrite(dyna.global_stress, sizeof(double), 2 * dyna.ndof, f);
+  fclose(f);
+  return 0;
+}
+'''
+
+
+@pytest.mark.gpu
+def test_reference_style_driver_j2_on_gpu(cilib, oracle, tmp_path):
+    """The drop-in Dynamics with force_law = CI_MODE_J2: 300 steps of a 20 m/s impact
+    that yields, against the FP64 run of the same formulation; its global_strains /
+    global_stress hold the reference's nodal fields (include/dynamics_kernels.h:117-147)
+    of the end state; VTK files at the reference's export steps carry them."""
+    m = mg.cube(4, 1)
+    inp = tmp_path / "m.inp"
+    mg.write_inp(m, str(inp))
+    exe = _compile(DRIVER_J2, tmp_path, "drvj2")
+    loc = float(m.xloc[:, 2].min()) - 1e-5
+    setup = mg.impact_setup(m, 20.0, 1e-5)
+    k, dt = setup["wall_stiffness"], setup["dt"]
+    out = tmp_path / "out"
+    out.mkdir()
+    state = tmp_path / "state.f64"
+    r = subprocess.run([str(exe), str(inp), repr(loc), repr(k), repr(dt), str(out), str(state)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    raw = np.fromfile(state)
+    n3 = m.xloc.size
+    x, v = raw[:n3].reshape(-1, 3), raw[n3:2 * n3].reshape(-1, 3)
+    eps, sig = raw[2 * n3:4 * n3].reshape(-1, 6), raw[4 * n3:].reshape(-1, 6)
+    par = oracle.params(68.9e9, 0.33, 2700.0, 60e6, 0.689e9, mode=oracle.J2,
+                        lumping=oracle.LUMP_HRZ, wall_normal=(0, 0, 1), wall_offset=loc,
+                        wall_stiffness=k)
+    o = oracle.Solver(m.xloc, m.conn, par)
+    o.initialize((0, 0, -20), dt)
+    o.step(300)
+    ref = o.get()
+    assert ref["epbar"].max() > 0
+    u_ref = ref["x"] - m.xloc
+    assert np.linalg.norm(x - m.xloc - u_ref) < 1e-3 * np.linalg.norm(u_ref)
+    assert np.linalg.norm(v - ref["v"]) < 1e-3 * np.linalg.norm(ref["v"])
+    rp = oracle.ref_params(68.9e9, 0.33, 2700.0, loc, k, 1)
+    eps_ref, sig_ref = oracle.ref_nodal_fields(m.xloc, x, m.conn, rp)
+    assert np.linalg.norm(eps - eps_ref) < 1e-5 * np.linalg.norm(eps_ref)
+    assert np.linalg.norm(sig - sig_ref) < 1e-5 * np.linalg.norm(sig_ref)
+    assert sorted(os.listdir(out)) == ["simulation_0.vtk", "simulation_150.vtk"]
+    text = (out / "simulation_150.vtk").read_text()
+    names = [ln.split()[1] for ln in text.splitlines() if ln.startswith("VECTORS")]
+    assert names == ["velocity", "strain1", "strain2", "stress1", "stress2", "acceleration", "mass"]

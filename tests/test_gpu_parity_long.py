@@ -135,3 +135,18 @@ def test_refcompat_trajectory_vs_reference_tet10(cilib):
     assert rel(st["x"] - g["xloc"], g["x"] - g["xloc"]) < TOL
     v0 = np.asarray(p["vel"], dtype=np.float64)
     assert rel(st["v"] - v0, g["v"] - v0) < TOL
+
+
+def test_shell_segment_tilted_wall_vs_fp64(cilib, oracle):
+    """The shell segment against a plane tilted by 5 degrees about the transverse axis
+    (normal (sin 5, 0, cos 5)), so one end lands first: 40 m/s, 1,500 steps."""
+    m = mg.shell(n_axial=20, L=4.0 * 20 / 140)
+    base = mg.impact_setup(m, 40.0, 0.0)
+    th = np.radians(5.0)
+    n = np.array([np.sin(th), 0.0, np.cos(th)])
+    setup = dict(base, wall_normal=tuple(n), wall_offset=float((m.xloc @ n).min() - 1e-4))
+    st, en, ref = run_pair(cilib, oracle, m, setup, 1500)
+    check_pair(m, setup, st, ref)
+    assert ref["epbar"].max() > 0
+    assert rel(st["epbar"], ref["epbar"]) < TOL
+    assert abs(en["balance"]) < 0.02 * en["kinetic0"]
