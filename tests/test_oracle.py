@@ -215,3 +215,24 @@ def test_j2_energy_balance(oracle, order):
     assert (st["contact"] & 2).sum() > 0  # and touches the wall
     assert en[oracle.E_PLASTIC] > 0.1 * en[oracle.E_KINETIC0]
     assert abs(en[oracle.E_BALANCE]) < 2e-3 * en[oracle.E_KINETIC0]
+
+
+@pytest.mark.parametrize("order,n", [(1, 5), (2, 3)])
+def test_fp64_solver_thread_count_independent(oracle, order, n):
+    """orc_step on 1, 3 and 8 threads gives the same bits: forces are summed per node in
+    element order and the work terms over fixed element blocks, whatever the threads."""
+    m = mg.cube(n, order)
+    setup = mg.impact_setup(m, 30.0, 1e-4)
+    par = oracle.params(E, NU, RHO, 100e6, 0.689e9, mode=oracle.J2, lumping=oracle.LUMP_HRZ,
+                        wall_normal=setup["wall_normal"], wall_offset=setup["wall_offset"],
+                        wall_stiffness=setup["wall_stiffness"])
+    outs = []
+    for th in (1, 3, 8):
+        o = oracle.Solver(m.xloc, m.conn, par, nthreads=th)
+        o.initialize(setup["vel"], setup["dt"])
+        o.step(150)
+        outs.append(o.get())
+    assert outs[0]["epbar"].max() > 0
+    for g in outs[1:]:
+        for k in ("x", "v", "sigma", "epbar", "energy", "contact"):
+            assert np.array_equal(g[k], outs[0][k]), k
