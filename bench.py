@@ -75,10 +75,12 @@ def workload(name: str):
     return m, setup, desc
 
 
-# DRAM bytes (read + write) per launch of the step kernel, from the ncu capture
-# summarised in profiles/k_step_qp10_shell_half.md (half shell, scaled x2 for the full
-# shell: elements and nodes double exactly).
-MEASURED_TRAFFIC = {"shell": 2 * 117.89e6, "shell_half": 117.89e6}
+# DRAM bytes (read + write) per step of the step kernel, from ncu captures: the task
+# kernel on the full shell (profiles/k_flow_qp10_shell.md: one launch of 20 steps,
+# divided by 20) and the fused kernel on the half shell (profiles/
+# k_step_qp10_shell_half.md, scaled x2 for the full shell: elements and nodes double).
+MEASURED_TRAFFIC = {("shell", 2): 7.751968e9 / 20, ("shell", 3): 2 * 117.89e6,
+                    ("shell_half", 3): 117.89e6}
 
 
 def algorithmic_bytes(npe: int, E: int, N: int):
@@ -300,16 +302,19 @@ def run_ours(args, rank, world):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    fused = args.step_kernel == 0
+    sk = s.step_kernel()  # the kernel the solver runs (0 = automatic resolved)
+    fused = sk != 1
     kbytes = step_bytes if fused else elem_bytes
     achieved = kbytes / (k_elem_ms * 1e-3) / 1e9
-    roofline = {"bound": "hbm",
-                "kernel": ("k_step (fused element force + J2 + assembly + node update)" if fused
-                           else "k_elem (element force + J2 + colour assembly)"),
+    kname = {0: "k_step (fused element force + J2 + assembly + node update)",
+             1: "k_elem (element force + J2 + colour assembly)",
+             2: "k_flow_qp10 (persistent task kernel: node and element tasks of every step)"}
+    kname[3] = kname[0]
+    roofline = {"bound": "hbm", "kernel": kname[sk],
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_src,
                 "traffic": (args.traffic if args.traffic is not None
-                            else MEASURED_TRAFFIC.get(args.workload) if fused else None),
+                            else MEASURED_TRAFFIC.get((args.workload, sk))),
                 "kernel_ms": round(k_elem_ms, 4),
                 "other_kernel_ms_per_step": round(k_node_ms, 4),
                 "bytes_formula": "E(4 npe + 56 nq) + 112 N" if fused else "E(4 npe + 56 nq) + 60 N"}
@@ -342,7 +347,9 @@ def run_ours(args, rank, world):
            "steps_per_call": S, "calls": calls,
            "api": "per call: ci_set_state(x, v) + ci_step(S) + ci_get_state(x, v), pinned host buffers"}
     en = s.energy()
-    launches = (s.launches_per_step() * args.steps + 1) * len(reps)
+    # fused path: one step kernel per step + the end-of-call completion per window; task
+    # kernel: one launch per window
+    launches = (1 if sk == 2 else s.launches_per_step() * args.steps + 1) * len(reps)
     s.close()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -619,7 +626,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default="shell",
                     choices=["shell", "shell_half", "quad", "small", "surrogate"])
-    ap.add_argument("--step-kernel", type=int, default=0, help="0 fused, 1 element + node kernels")
+    ap.add_argument("--step-kernel", type=int, default=0,
+                    help="0 automatic, 1 element + node kernels, 2 persistent task kernel "
+                         "(tet10), 3 fused")
     ap.add_argument("--chunk-elements", type=int, default=0)
     ap.add_argument("--chunk-nodes", type=int, default=0)
     ap.add_argument("--block-threads", type=int, default=0)

@@ -100,6 +100,7 @@ EXPORTS = {
     "ci_time_steps": (C.c_int, [C.c_void_p, C.c_int, _fp]),
     "ci_time_kernels": (C.c_int, [C.c_void_p, C.c_int, _fp]),
     "ci_launches_per_step": (C.c_int, [C.c_void_p]),
+    "ci_step_kernel": (C.c_int, [C.c_void_p]),
     "ci_mesh_load_inp": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(CiMesh)]),
     "ci_mesh_free": (None, [C.POINTER(CiMesh)]),
     "ci_plan_stats": (C.c_int, [C.POINTER(CiMesh), C.c_int, C.c_int, C.POINTER(C.c_longlong),
@@ -353,6 +354,11 @@ class Solver:
 
     def launches_per_step(self) -> int:
         return lib().ci_launches_per_step(self._h)
+
+    def step_kernel(self) -> int:
+        """The step kernel this solver runs: 1 element + node kernels, 2 persistent task
+        kernel, 3 fused (the automatic choice of step_kernel=0 resolved)."""
+        return lib().ci_step_kernel(self._h)
 
 
 class Batch:

@@ -29,7 +29,7 @@ namespace ci {
 
 enum ElemMode { EM_J2 = 0, EM_REFCOMPAT = 1, EM_MASS_ROWSUM = 2, EM_MASS_HRZ = 3 };
 
-enum StatusBits { ST_DEGENERATE = 1u, ST_NONFINITE = 2u };
+enum StatusBits { ST_DEGENERATE = 1u, ST_NONFINITE = 2u, ST_FLOW_TIMEOUT = 8u };
 
 struct DevPlan {
   const ChunkInfo* chunks;
@@ -801,16 +801,17 @@ __device__ __forceinline__ void node_epilogue(const FusedArgs& A, const ChunkInf
   }
 }
 
-// The CTA's internal and plastic work of this step added to chunk c's running sums.
-template <int BS>
+// The CTA's internal and plastic work of this step added to chunk c's running sums
+// (CG: read them through L2 only, for kernels in which another SM wrote them last).
+template <int BS, bool CG = false>
 __device__ __forceinline__ void add_chunk_work(const FusedArgs& A, int c, float wint, float wp,
                                                float* red) {
   const float t0 = block_sum<BS>(wint, red);
   const float t1 = block_sum<BS>(wp, red);
   if (threadIdx.x == 0) {
     double* cw = A.chunk_work + 4 * (size_t)c;
-    cw[0] += (double)t0;
-    cw[1] += (double)t1;
+    cw[0] = (CG ? __ldcg(cw) : cw[0]) + (double)t0;
+    cw[1] = (CG ? __ldcg(cw + 1) : cw[1]) + (double)t1;
   }
 }
 
@@ -1029,8 +1030,10 @@ __device__ __forceinline__ void tet10_rs_slot(const Tet10QP& t, const float (&Pm
 
 // Element loop of one chunk by the CTA's BS threads (4 lanes per element, colours
 // applied in order between barriers), then the chunk's partial nodal forces to the halo
-// and its work to chunk c's sums.
-template <int MODE, int BS>
+// and its work to chunk c's sums.  CG: the stored stress, plastic strain and work sums
+// are read through L2 only (the persistent task kernel, where another SM may have
+// written them last).
+template <int MODE, int BS, bool CG = false>
 __device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const ElemParams& ep,
                                                    const ChunkInfo& ch, const Tile& T, int tid,
                                                    int c, float* red) {
@@ -1053,9 +1056,9 @@ __device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const Ele
     float2 s2 = make_float2(0.f, 0.f);
     float ep0 = 0.f;
     if (MODE == EM_J2) {
-      s4 = A.sig_a[qi];
-      s2 = A.sig_b[qi];
-      ep0 = A.epbar[qi];
+      s4 = CG ? __ldcg(A.sig_a + qi) : A.sig_a[qi];
+      s2 = CG ? __ldcg(A.sig_b + qi) : A.sig_b[qi];
+      ep0 = CG ? __ldcg(A.epbar + qi) : A.epbar[qi];
     }
     float2 JG[9];
 #pragma unroll
@@ -1169,7 +1172,7 @@ __device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const Ele
   }
   __syncthreads();
   node_epilogue<BS>(A, ch, T, tid);
-  if (ep.accum_energy) add_chunk_work<BS>(A, c, wint, wp, red);
+  if (ep.accum_energy) add_chunk_work<BS, CG>(A, c, wint, wp, red);
 }
 
 // 6 CTAs of 128 threads per SM (80 registers) fit the 896-node chunk's shared tile
@@ -1187,6 +1190,271 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
   if (cs.mode == 1) return;
   __syncthreads();
   step_qp10_elements<MODE, BS>(A, cs.ep, ch, T, threadIdx.x, blockIdx.x, red);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent task kernel of the four-lane tet10 step (step_kernel = 2).
+//
+// A call of n steps is one launch whose CTAs claim tasks from a counter, in the order
+//   N(0, c) for every chunk c;  then for j = 0 .. n-1:  E(j, c) for every c, N(j+1, c) for every c.
+// N(j, c): chunk c completes S^j of the nodes it owns -- from S^{j-1} and the halo of step
+//   j-1 exactly as the fused kernel's staging does (N(0) reads the state as it is, N(n)
+//   also stores the accelerations) -- and writes each node's record (u and dt v rounded to
+//   FP32) to the record buffers of parity j.
+// E(j, c): chunk c stages its local nodes from those records (x = chunk-relative X0 + u,
+//   the fused kernel's sum) and runs the element loop of step j, writing its halo partials
+//   (parity j), stored stress and work sums.
+// E(j, c) waits until every chunk owning one of c's nodes has finished N(j, .); N(j, c)
+// waits until every chunk with a slot of one of c's nodes has finished E(j-1, .).  These
+// waits order every reuse of the double buffers (records, halo, state) as well: E(j-2, t)
+// precedes N(j-1, c) precedes E(j-1, t) precedes N(j, c) for any chunk t touching c.  Every
+// dependency of a task comes earlier in the claim order and a claimed task runs on a
+// resident CTA, so the earliest unfinished task can always proceed.  Each node is
+// completed once (no ghost copies), and CTAs doing node tasks (memory and FP64 bound)
+// share the SMs with CTAs doing element tasks (FP32 issue bound).  The arithmetic is
+// the fused kernel's, so the results are the same bits.
+//
+// Data written by other CTAs of the launch (records, halo, state, stored stress, work
+// sums, contact flags) is read through L2 only (ld.global.cg), never from a possibly
+// stale L1 line.  A task publishes its completion with a release store after a
+// __threadfence; the lanes of warp 0 read a task's neighbours' counters with acquire
+// loads, one neighbour per lane.  Every wait is bounded
+// in time (kFlowWaitNs): past it the CTA sets ST_FLOW_TIMEOUT and the abort flag, and
+// every CTA stops at its next claim or wait.
+struct FlowArgs {
+  FusedArgs A[2];        // buffers of an even / odd step: state cur/prv, halo cur/prv
+  float4* rec_a[2];      // per node and parity: (u_x, u_y, u_z, dt v_x) in FP32
+  float2* rec_b[2];      //                       (dt v_y, dt v_z)
+  const int* own_row;    // chunks owning a local node of chunk c: own_idx[own_row[c] ..]
+  const int* own_idx;
+  const int* touch_row;  // chunks with a slot of a node chunk c owns: touch_idx[touch_row[c] ..]
+  const int* touch_idx;
+  int* node_done;        // [C] last j whose N(j, c) finished (-1 before the first)
+  int* elem_done;        // [C] last j whose E(j, c) finished
+  int* task_ctr;
+  int* abort_flag;
+  int C;
+  int nsteps;
+};
+
+constexpr unsigned long long kFlowWaitNs = 2000000000ull;  // 2 s without the awaited progress
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Warp 0: wait until ctr[idx[k]] >= target for every k in [b, e), lane l polling entries
+// l, l + 32, ... at once (one round trip to L2 for a typical task's 5 - 10 neighbours);
+// false on abort or timeout (the same on every lane).
+__device__ __forceinline__ bool flow_wait(const FlowArgs& F, const int* ctr, const int* idx, int b,
+                                          int e, int target) {
+  const int lane = threadIdx.x & 31;
+  bool ok = true;
+  unsigned long long t0 = 0;
+  for (int k = b + lane; k < e && ok; k += 32) {
+    const int* p = ctr + idx[k];
+    for (unsigned spins = 0; ld_acquire(p) < target; spins++) {
+      if (spins >= 4) __nanosleep(128);
+      if ((spins & 31u) == 31u) {
+        if (*(volatile int*)F.abort_flag) {
+          ok = false;
+          break;
+        }
+        const unsigned long long t = global_ns();
+        if (t0 == 0) t0 = t;
+        if (t - t0 > kFlowWaitNs) {
+          atomicOr(F.A[0].status, (unsigned)ST_FLOW_TIMEOUT);
+          atomicExch(F.abort_flag, 1);
+          ok = false;
+          break;
+        }
+      }
+    }
+  }
+  return __all_sync(0xffffffffu, ok);
+}
+
+// Thread 0 after the CTA's writes and a barrier: publish ctr[c] = j.
+__device__ __forceinline__ void flow_publish(int* ctr, int c, int j) {
+  __threadfence();
+  st_release(ctr + c, j);
+}
+
+// N(j, c): S^j of the nodes chunk c owns and their records.  Each thread takes KN nodes
+// at a time and issues all their loads before the first update (the node task has the
+// registers the element task needs to spare); every node's arithmetic is the fused
+// kernel's staging.
+template <int BS>
+__device__ __forceinline__ void flow_nodes(const FlowArgs& F, const ElemParams& ep,
+                                           const NodeParams& np, const ChunkInfo& ch, int j) {
+  constexpr int KN = 2;
+  const FusedArgs& A = F.A[j & 1];
+  const DevPlan& P = A.P;
+  float4* ra = F.rec_a[j & 1];
+  float2* rb = F.rec_b[j & 1];
+  const bool last = j == F.nsteps;
+  for (int l0 = threadIdx.x; l0 < ch.n_own; l0 += KN * BS) {
+    float uf[KN][3], vf[KN][3];
+    if (j == 0) {
+#pragma unroll
+      for (int q = 0; q < KN; q++) {
+        const int g = ch.own_begin + min(l0 + q * BS, ch.n_own - 1);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          uf[q][k] = f64_to_f32(__ldcg(A.u_cur[k] + g));
+          vf[q][k] = f64_to_f32(__ldcg(A.v_cur[k] + g));
+        }
+      }
+    } else {
+      // past the end: repeat the last owned node (loads only, results unused)
+      int g[KN], s0[KN], s1[KN];
+#pragma unroll
+      for (int q = 0; q < KN; q++) {
+        const int l = min(l0 + q * BS, ch.n_own - 1);
+        g[q] = ch.own_begin + l;
+        if (l < ch.n_int) {
+          s0[q] = ch.slot_begin + l;
+          s1[q] = s0[q] + 1;
+        } else {
+          const int2 r = P.local_srow[ch.local_begin + l];
+          s0[q] = r.x;
+          s1[q] = r.y;
+        }
+      }
+      float f[KN][3], m[KN], d0f[KN];
+      double u[KN][3], v[KN][3];
+      unsigned char ct[KN];
+#pragma unroll
+      for (int q = 0; q < KN; q++) {
+        const bool two = s1[q] > s0[q] + 1;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          const float h0 = __ldcg(A.halo_prv[k] + s0[q]);
+          const float h1 = two ? __ldcg(A.halo_prv[k] + s0[q] + 1) : 0.f;
+          f[q][k] = __fadd_rn(0.f, h0);
+          if (two) f[q][k] = __fadd_rn(f[q][k], h1);
+          u[q][k] = __ldcg(A.u_prv[k] + g[q]);
+          v[q][k] = __ldcg(A.v_prv[k] + g[q]);
+        }
+        m[q] = A.mass[g[q]];
+        d0f[q] = A.d0f[g[q]];
+        ct[q] = __ldcg(A.contact + g[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < KN; q++)
+        for (int sl = s0[q] + 2; sl < s1[q]; sl++) {
+#pragma unroll
+          for (int k = 0; k < 3; k++) f[q][k] = __fadd_rn(f[q][k], __ldcg(A.halo_prv[k] + sl));
+        }
+#pragma unroll
+      for (int q = 0; q < KN; q++) {
+        if (l0 + q * BS >= ch.n_own) break;
+        float a[3];
+        bool hit;
+        node_step(np, f[q][0], f[q][1], f[q][2], m[q], d0f[q], A.d0, g[q], u[q], v[q], a, hit,
+                  uf[q], vf[q]);
+        store_node(A, A.u_cur, A.v_cur, g[q], u[q], v[q], vf[q], a, hit, last, ct[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < KN; q++) {
+      const int l = l0 + q * BS;
+      if (l >= ch.n_own) break;
+      const int g = ch.own_begin + l;
+      ra[g] = make_float4(uf[q][0], uf[q][1], uf[q][2], ep.dt * vf[q][0]);
+      rb[g] = make_float2(ep.dt * vf[q][1], ep.dt * vf[q][2]);
+    }
+  }
+}
+
+// E(j, c): the chunk's local nodes from the records of step j into the tile.
+template <int BS>
+__device__ __forceinline__ void flow_stage(const FlowArgs& F, const ChunkInfo& ch, const Tile& T,
+                                           int j) {
+  const DevPlan& P = F.A[0].P;
+  const float4* ra = F.rec_a[j & 1];
+  const float2* rb = F.rec_b[j & 1];
+  for (int l = threadIdx.x; l < ch.n_local; l += BS) {
+    const int lb = ch.local_begin + l;
+    const int g = l < ch.n_own ? ch.own_begin + l : P.local_gid[lb];
+    const float4 r0 = __ldcg(ra + g);
+    const float2 r1 = __ldcg(rb + g);
+    float x0[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) x0[k] = P.local_x0[k * (size_t)P.Lt + lb];
+    store_record(T, l, x0[0] + r0.x, x0[1] + r0.y, x0[2] + r0.z, r0.w, r1.x, r1.y);
+    T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+template <int MODE, int BS>
+__global__ void __launch_bounds__(BS, 768 / BS) k_flow_qp10(FlowArgs F, ElemParams ep,
+                                                          NodeParams np) {
+  extern __shared__ float sm[];
+  __shared__ float red[BS / 32];
+  __shared__ int sh_task, sh_next, sh_ok;
+  const int C = F.C;
+  const long long ntasks = (long long)C + 2LL * C * F.nsteps;
+  // the next task is claimed while the current one runs (one atomic round trip hidden);
+  // a claimed task waits only for tasks earlier in the claim order, so holding it is safe
+  if (threadIdx.x == 0) sh_next = atomicAdd(F.task_ctr, 1);
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      sh_task = *(volatile int*)F.abort_flag ? -1 : sh_next;
+      if (sh_task >= 0 && sh_task < ntasks) sh_next = atomicAdd(F.task_ctr, 1);
+    }
+    __syncthreads();
+    const int t = sh_task;
+    if (t < 0 || t >= ntasks) break;
+    int j, c;
+    bool elem;
+    if (t < C) {
+      j = 0;
+      c = t;
+      elem = false;
+    } else {
+      const int r = (t - C) % (2 * C);
+      j = (t - C) / (2 * C);
+      elem = r < C;
+      c = elem ? r : r - C;
+      if (!elem) j++;
+    }
+    const DevPlan& P = F.A[0].P;
+    const ChunkInfo ch = P.chunks[c];
+    if (threadIdx.x < 32) {
+      const bool ok = elem ? flow_wait(F, F.node_done, F.own_idx, F.own_row[c], F.own_row[c + 1], j)
+                           : (j == 0 || flow_wait(F, F.elem_done, F.touch_idx, F.touch_row[c],
+                                                  F.touch_row[c + 1], j - 1));
+      if (threadIdx.x == 0) sh_ok = ok;
+    }
+    __syncthreads();
+    if (!sh_ok) break;
+    if (elem) {
+      const Tile T = make_tile(sm, ch.n_local);
+      flow_stage<BS>(F, ch, T, j);
+      __syncthreads();
+      step_qp10_elements<MODE, BS, true>(F.A[j & 1], ep, ch, T, threadIdx.x, c, red);
+      __syncthreads();
+      if (threadIdx.x == 0) flow_publish(F.elem_done, c, j);
+    } else {
+      flow_nodes<BS>(F, ep, np, ch, j);
+      __syncthreads();
+      if (threadIdx.x == 0) flow_publish(F.node_done, c, j);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -119,6 +119,14 @@ struct ci_solver {
   // the plan index of every caller node, and [3N] AoS staging buffers
   DBuf<double> d_Xc, d_xc, d_vc;
   DBuf<int> d_node_new;
+  // persistent task kernel (step_kernel = 2): node records of the two parities, the
+  // owner / toucher lists of every chunk, per-chunk progress counters, the task counter
+  // and the abort flag ([2C + 2] ints), and the CTAs it keeps resident
+  DBuf<float4> d_rec_a[2];
+  DBuf<float2> d_rec_b[2];
+  DBuf<int> d_own_row, d_own_idx, d_touch_row, d_touch_idx, d_flow_ctr;
+  int flow_ctas = 0;
+  std::vector<int> own_row, own_idx, touch_row, touch_idx;  // host copies
   bool xc_stale = true;  // X changed since d_Xc was uploaded
   // nodal strain/stress output: last element (caller order) of every node, and the plan
   // position of every caller element (built on first use)
@@ -261,6 +269,14 @@ cudaError_t configure_step(int bytes) {
     if ((e = cudaFuncSetAttribute(ci::k_step_qp10<ci::EM_REFCOMPAT, BS>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
       return e;
+    if (BS == 128) {
+      if ((e = cudaFuncSetAttribute(ci::k_flow_qp10<ci::EM_J2, 128>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+      if ((e = cudaFuncSetAttribute(ci::k_flow_qp10<ci::EM_REFCOMPAT, 128>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    }
   }
   return cudaFuncSetAttribute(ci::k_step<NPE, ci::EM_REFCOMPAT, BS>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -392,6 +408,8 @@ int check_status(ci_solver* s) {
   CI_CUDA(cudaStreamSynchronize(s->stream));
   if (st & ci::ST_DEGENERATE) return fail(CI_ERR_DEGENERATE, "an element has det J <= 0");
   if (st & ci::ST_NONFINITE) return fail(CI_ERR_NONFINITE, "non-finite nodal state");
+  if (st & ci::ST_FLOW_TIMEOUT)
+    return fail(CI_ERR_CUDA, "step task kernel: a task waited longer than its time limit");
   return CI_OK;
 }
 
@@ -481,7 +499,7 @@ void destroy_graph(ci_solver* s) {
   s->graph_steps = 0;
 }
 
-bool fused_path(const ci_solver* s) { return s->opt.step_kernel == 0; }
+bool fused_path(const ci_solver* s) { return s->opt.step_kernel == 3; }
 
 int capture(ci_solver* s, cudaGraphExec_t* out, int steps, bool first) {
   cudaGraph_t g = nullptr;
@@ -515,9 +533,114 @@ int build_graph(ci_solver* s, int steps) {
   return CI_OK;
 }
 
+template <typename T>
+int upload(DBuf<T>& b, const std::vector<T>& h, cudaStream_t st);
+
+// Task kernel (step_kernel = 2): for every chunk the chunks owning one of its local
+// nodes (whose node tasks its element task waits for) and the chunks holding a slot of
+// a node it owns (whose element tasks its node task waits for), as CSR lists; record
+// buffers, counters and the number of CTAs kept resident.
+int setup_flow(ci_solver* s) {
+  const ci::Plan& P = s->plan;
+  const int C = s->C;
+  std::vector<int> owner(s->N, -1);
+  for (int c = 0; c < C; c++)
+    for (int l = 0; l < P.chunks[c].n_own; l++) owner[P.chunks[c].own_begin + l] = c;
+  std::vector<std::vector<int>> own(C), touch(C);
+  for (int c = 0; c < C; c++) {
+    const ci::ChunkInfo& ch = P.chunks[c];
+    for (int l = 0; l < ch.n_local; l++) {
+      const int g = l < ch.n_own ? ch.own_begin + l : P.local_gid[ch.local_begin + l];
+      own[c].push_back(owner[g]);
+      touch[owner[g]].push_back(c);
+    }
+  }
+  auto csr = [](std::vector<std::vector<int>>& lists, std::vector<int>* row, std::vector<int>* idx) {
+    row->assign(1, 0);
+    idx->clear();
+    for (auto& v : lists) {
+      std::sort(v.begin(), v.end());
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+      idx->insert(idx->end(), v.begin(), v.end());
+      row->push_back((int)idx->size());
+    }
+  };
+  csr(own, &s->own_row, &s->own_idx);
+  csr(touch, &s->touch_row, &s->touch_idx);
+  int rc;
+  if ((rc = upload(s->d_own_row, s->own_row, s->stream))) return rc;
+  if ((rc = upload(s->d_own_idx, s->own_idx, s->stream))) return rc;
+  if ((rc = upload(s->d_touch_row, s->touch_row, s->stream))) return rc;
+  if ((rc = upload(s->d_touch_idx, s->touch_idx, s->stream))) return rc;
+  for (int p = 0; p < 2; p++) {
+    CI_CUDA(s->d_rec_a[p].alloc(s->N));
+    CI_CUDA(s->d_rec_b[p].alloc(s->N));
+  }
+  CI_CUDA(s->d_flow_ctr.alloc(2 * (size_t)C + 2));
+  int per_sm = 0, sms = 0;
+  CI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, s->opt.mode != CI_MODE_REFCOMPAT ? ci::k_flow_qp10<ci::EM_J2, 128>
+                                                : ci::k_flow_qp10<ci::EM_REFCOMPAT, 128>,
+      128, s->smem_bytes));
+  CI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+  s->flow_ctas = std::max(1, std::min(per_sm * sms, C));
+  return CI_OK;
+}
+
+// n steps in launches of the task kernel (at most kFlowMaxSteps steps each, so the task
+// count fits an int), each from a complete state in buffer A to a complete state in A.
+constexpr int kFlowMaxSteps = 1 << 16;
+
+cudaError_t enqueue_flow(ci_solver* s, int n) {
+  const int C = s->C;
+  const ci::ElemParams ep = s->elem_params((float)s->dt, true);
+  const ci::NodeParams np = s->node_params();
+  for (int done = 0; done < n;) {
+    const int k = std::min(n - done, kFlowMaxSteps);
+    ci::FlowArgs F;
+    F.A[0] = s->fused_args(true, 0, false, false);
+    F.A[1] = s->fused_args(false, 1, false, false);
+    for (int p = 0; p < 2; p++) {
+      F.rec_a[p] = s->d_rec_a[p].p;
+      F.rec_b[p] = s->d_rec_b[p].p;
+    }
+    F.own_row = s->d_own_row.p;
+    F.own_idx = s->d_own_idx.p;
+    F.touch_row = s->d_touch_row.p;
+    F.touch_idx = s->d_touch_idx.p;
+    F.node_done = s->d_flow_ctr.p;
+    F.elem_done = s->d_flow_ctr.p + C;
+    F.task_ctr = s->d_flow_ctr.p + 2 * C;
+    F.abort_flag = s->d_flow_ctr.p + 2 * C + 1;
+    F.C = C;
+    F.nsteps = k;
+    cudaError_t e;
+    // progress counters to -1, task counter and abort flag to 0
+    if ((e = cudaMemsetAsync(s->d_flow_ctr.p, 0xff, sizeof(int) * 2 * (size_t)C, s->stream))) return e;
+    if ((e = cudaMemsetAsync(F.task_ctr, 0, 2 * sizeof(int), s->stream))) return e;
+    if (s->opt.mode != CI_MODE_REFCOMPAT)
+      ci::k_flow_qp10<ci::EM_J2, 128><<<s->flow_ctas, 128, s->smem_bytes, s->stream>>>(F, ep, np);
+    else
+      ci::k_flow_qp10<ci::EM_REFCOMPAT, 128><<<s->flow_ctas, 128, s->smem_bytes, s->stream>>>(F, ep, np);
+    if ((e = cudaGetLastError())) return e;
+    if (k & 1) {
+      const size_t b = sizeof(double) * 3 * (size_t)s->N;
+      if ((e = cudaMemcpyAsync(s->d_u.p, s->d_ub.p, b, cudaMemcpyDeviceToDevice, s->stream))) return e;
+      if ((e = cudaMemcpyAsync(s->d_v.p, s->d_vb.p, b, cudaMemcpyDeviceToDevice, s->stream))) return e;
+    }
+    done += k;
+  }
+  return cudaSuccess;
+}
+
 // Enqueue n steps; the last stores the acceleration for energy read-back.
 int enqueue_steps(ci_solver* s, int n) {
   if (n <= 0) return CI_OK;
+  if (s->opt.step_kernel == 2) {
+    CI_CUDA(enqueue_flow(s, n));
+    s->steps_done += n;
+    return CI_OK;
+  }
   if (fused_path(s)) {
     // chained graphs of G (even) steps, then the remainder directly and the completion
     const int G = (s->opt.graph_steps > 0 ? s->opt.graph_steps : 32) & ~1;
@@ -815,10 +938,14 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
     ci_default_options(&s->opt);
   if (s->opt.mode != CI_MODE_J2 && s->opt.mode != CI_MODE_REFCOMPAT)
     return fail(CI_ERR_INVALID, "unknown mode");
-  if (s->opt.step_kernel != 0 && s->opt.step_kernel != 1)
+  if (s->opt.step_kernel < 0 || s->opt.step_kernel > 3)
     return fail(CI_ERR_INVALID, "unknown step_kernel");
   if (s->opt.block_threads == 0) s->opt.block_threads = 128;
   if (s->opt.elem_lanes == 0) s->opt.elem_lanes = 4;
+  if (s->opt.step_kernel == 2 &&
+      (mesh->nodes_per_element != 10 || s->opt.elem_lanes != 4 || s->opt.block_threads != 128))
+    return fail(CI_ERR_UNSUPPORTED,
+                "step_kernel 2 (task kernel) needs tet10, elem_lanes 4 and block_threads 128");
   if (s->opt.elem_lanes != 1 && s->opt.elem_lanes != 4)
     return fail(CI_ERR_INVALID, "elem_lanes must be 1 or 4");
   if (s->opt.block_threads != 64 && s->opt.block_threads != 128 && s->opt.block_threads != 256)
@@ -850,6 +977,20 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   s->vel0.assign(3, 0.0);
 
   CI_CUDA(s->npe == 4 ? configure_npe<4>((int)s->smem_bytes) : configure_npe<10>((int)s->smem_bytes));
+  if (s->opt.step_kernel == 0) {
+    // automatic: the task kernel when the chunks of a four-lane tet10 mesh need more than
+    // 1.5 rounds of the fused kernel's resident CTAs (it then hides the lock-step of node
+    // staging and element loops; on meshes of about one round its waits cost more), else
+    // the fused kernel.  Both give the same bits.
+    s->opt.step_kernel = 3;
+    if (s->npe == 10 && s->opt.elem_lanes == 4 && s->opt.block_threads == 128) {
+      int per_sm = 0, sms = 0;
+      CI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, ci::k_step_qp10<ci::EM_J2, 128>, 128, s->smem_bytes));
+      CI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+      if (2LL * s->C > 3LL * per_sm * sms) s->opt.step_kernel = 2;
+    }
+  }
   CI_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   CI_CUDA(cudaEventCreate(&s->ev0));
   CI_CUDA(cudaEventCreate(&s->ev1));
@@ -866,11 +1007,12 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   CI_CUDA(s->d_u.alloc(3 * N));
   CI_CUDA(s->d_v.alloc(3 * N));
   CI_CUDA(s->d_slot.alloc(3 * (size_t)s->S));
-  if (s->opt.step_kernel == 0) {
+  if (s->opt.step_kernel == 3 || s->opt.step_kernel == 2) {
     CI_CUDA(s->d_ub.alloc(3 * N));
     CI_CUDA(s->d_vb.alloc(3 * N));
     CI_CUDA(s->d_halo1.alloc(3 * (size_t)s->S));
   }
+  if (s->opt.step_kernel == 2 && (rc = setup_flow(s.get()))) return rc;
   CI_CUDA(s->d_mass.alloc(N));
   CI_CUDA(s->d_d0.alloc(N));
   CI_CUDA(s->d_d0f.alloc(N));
@@ -1426,7 +1568,16 @@ int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms) {
   std::vector<cudaEvent_t> ev(3 * nsteps);
   for (auto& e : ev) CI_CUDA(cudaEventCreate(&e));
   double te = 0, tn = 0;
-  if (fused_path(s)) {
+  if (s->opt.step_kernel == 2) {
+    // one launch runs all the steps: out[0] = its duration per step, out[1] = 0
+    CI_CUDA(cudaEventRecord(ev[0], s->stream));
+    CI_CUDA(enqueue_flow(s, nsteps));
+    CI_CUDA(cudaEventRecord(ev[1], s->stream));
+    CI_CUDA(cudaEventSynchronize(ev[1]));
+    float a;
+    CI_CUDA(cudaEventElapsedTime(&a, ev[0], ev[1]));
+    te = a;
+  } else if (fused_path(s)) {
     // out[0]: mean k_step duration; out[1]: the end-of-call boundary finalise
     for (int i = 0; i < nsteps; i++) {
       const ci::FusedArgs F = s->fused_args((i & 1) == 0, i & 1, i == 0, false);
@@ -1478,7 +1629,12 @@ int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms) {
   return check_status(s);
 }
 
-int ci_launches_per_step(const ci_solver* s) { return s ? (s->opt.step_kernel == 0 ? 1 : 2) : 0; }
+int ci_step_kernel(const ci_solver* s) { return s ? s->opt.step_kernel : -1; }
+
+int ci_launches_per_step(const ci_solver* s) {
+  // the task kernel launches once per call of any length (and per 65,536 steps)
+  return s ? (s->opt.step_kernel == 1 ? 2 : 1) : 0;
+}
 
 int ci_plan_stats(const ci_mesh* mesh, int chunk_elements, int chunk_nodes, long long* stats,
                   int* perm_elems, int* perm_nodes) {

@@ -94,7 +94,11 @@ typedef struct ci_options {
   int chunk_elements; /* elements per CTA chunk, 0 = automatic */
   int chunk_nodes;    /* local-node budget per chunk, 0 = automatic */
   int graph_steps;    /* steps captured per CUDA graph, 0 = automatic */
-  int step_kernel;    /* 0 = fused (one launch per step, default), 1 = element + node kernels */
+  int step_kernel;    /* 0 = automatic (2 for four-lane tet10 meshes of more than 1.5 rounds of
+                         fused CTAs, else 3), 1 = element + node kernels, 2 = persistent task
+                         kernel (tet10, elem_lanes 4, block_threads 128: node and element
+                         tasks of all the call's steps), 3 = fused (one launch per step);
+                         0, 2 and 3 give the same bits */
   int block_threads;  /* threads per chunk CTA of the fused kernel: 64, 128 or 256; 0 = automatic */
   int elem_lanes;     /* tet10 fused kernel: 4 = one lane per Gauss point, 1 = one thread per
                          element; 0 = automatic (4) */
@@ -320,8 +324,11 @@ int ci_time_steps(ci_solver* s, int nsteps, float* ms);
  * finalise divided by nsteps (its share per step); two-kernel path out[0] = element
  * kernel, out[1] = node kernel. */
 int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms);
-/* Kernel launches one step issues (for launch accounting). */
+/* Kernel launches one step issues (for launch accounting; the task kernel launches once
+ * per call of up to 65,536 steps). */
 int ci_launches_per_step(const ci_solver* s);
+/* The step kernel a solver runs (ci_options::step_kernel with 0 resolved), -1 for NULL. */
+int ci_step_kernel(const ci_solver* s);
 
 /* ---- mesh utilities (host only) ---- */
 /* Mesh::load_mesh (include/mesh.h:57-267): parse an Abaqus/CalculiX .inp file.

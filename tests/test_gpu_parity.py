@@ -360,3 +360,53 @@ def test_nodal_fields_match_reference_output(cilib, oracle, order, n):
     assert rel(fld["stress"], sig_ref) < 1e-5
     acc_fd = (st["v"] - v_prev) / setup["dt"]
     assert rel(fld["acc"], acc_fd) < 1e-5
+
+
+@pytest.mark.parametrize("mesh,mode,speed,calls", [
+    ("cube3", "j2", 20.0, (37, 20)), ("cube6", "j2", 30.0, (1, 64, 15)),
+    ("cube4", "refcompat", 20.0, (40,)), ("shellseg", "j2", 40.0, (25, 24))])
+def test_task_kernel_bitwise_equal_to_fused(cilib, mesh, mode, speed, calls):
+    """step_kernel = 2 (the persistent task kernel: node tasks and element tasks claimed
+    from a counter, each waiting only for its neighbours' progress) computes the fused
+    kernel's arithmetic, so every state array ends with the same bits, over calls of odd
+    and even length."""
+    m = (mg.shell(n_axial=6, L=4.0 * 6 / 140) if mesh == "shellseg"
+         else mg.cube(int(mesh[4:]), 2))
+    setup = mg.impact_setup(m, speed, 0.0 if mesh == "shellseg" else 1e-4)
+    md = cilib.MODE_J2 if mode == "j2" else cilib.MODE_REFCOMPAT
+    out = []
+    for sk in (3, 2):
+        # HRZ masses in both laws (tet10 row-sum corner masses are negative)
+        s = solver(cilib, m, md, lumping=cilib.LUMP_HRZ, wall_normal=setup["wall_normal"],
+                   wall_offset=setup["wall_offset"], wall_stiffness=setup["wall_stiffness"],
+                   step_kernel=sk)
+        s.initialize(setup["vel"])
+        s.start(setup["dt"])
+        for n in calls:
+            s.step(n)
+        out.append((s.state(), s.energy()))
+        s.close()
+    (a, ea), (b, eb) = out
+    for k in ("x", "v", "sigma", "epbar", "contact"):
+        assert np.array_equal(a[k], b[k]), k
+    assert ea["internal"] == eb["internal"] and ea["kinetic"] == eb["kinetic"]
+
+
+def test_task_kernel_rejects_other_element_types(cilib):
+    m = mg.cube(3, 1)
+    with pytest.raises(cilib.CiError) as e:
+        solver(cilib, m, cilib.MODE_J2, step_kernel=2)
+    assert e.value.code == -5
+
+
+def test_step_kernel_automatic_choice(cilib):
+    """step_kernel = 0 picks the fused kernel for a mesh of about one round of CTAs and
+    the task kernel for a tet10 mesh of many (the full shell: 1,736 chunks)."""
+    small = mg.cube(4, 2)
+    s = solver(cilib, small, cilib.MODE_J2)
+    assert s.step_kernel() == 3
+    s.close()
+    shell = mg.shell()
+    s = solver(cilib, shell, cilib.MODE_J2)
+    assert s.step_kernel() == 2
+    s.close()
