@@ -196,7 +196,7 @@ def plan_stats(xloc, conn, chunk_elements=0, chunk_nodes=0, perms=False):
                               None if pe is None else pe.ctypes.data_as(_ip),
                               None if pn is None else pn.ctypes.data_as(_ip)))
     keys = ["chunks", "max_colors", "max_local", "slots", "max_chunk_elems", "ghosts",
-            "boundary_nodes"]
+            "boundary_nodes", "max_task_deps"]
     out = {k: int(st[i]) for i, k in enumerate(keys)}
     if perms:
         out["perm_elems"], out["perm_nodes"] = pe, pn

@@ -1029,37 +1029,54 @@ __device__ __forceinline__ void tet10_rs_slot(const Tet10QP& t, const float (&Pm
 }
 
 // Element loop of one chunk by the CTA's BS threads (4 lanes per element, colours
-// applied in order between barriers), then the chunk's partial nodal forces to the halo
-// and its work to chunk c's sums.  CG: the stored stress, plastic strain and work sums
-// are read through L2 only (the persistent task kernel, where another SM may have
-// written them last).
-template <int MODE, int BS, bool CG = false>
-__device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const ElemParams& ep,
-                                                   const ChunkInfo& ch, const Tile& T, int tid,
-                                                   int c, float* red) {
+// applied in order between barriers) into the tile's force accumulators; this thread's
+// internal and plastic work in wint, wp.  CG: the stored stress and plastic strain are
+// read through L2 only (the persistent task kernel, where another SM may have written
+// them last).  PF: the next window's connectivity, stored stress and colours are loaded
+// before the current window's colour loop (where few registers are live), so that their
+// round trip overlaps the accumulation instead of stalling the next window's gather.
+template <int MODE, int BS, bool CG, bool PF>
+__device__ __forceinline__ void qp10_element_loop(const FusedArgs& A, const ElemParams& ep,
+                                                  const ChunkInfo& ch, const Tile& T, int tid,
+                                                  float& wint, float& wp) {
   const DevPlan& P = A.P;
   const int q = tid & 3;
   const Tet10QP t = tet10_qp(q);
   constexpr float W = 1.0f / 24.0f;
   const int E = P.E;
-  float wint = 0.f, wp = 0.f;
+  wint = 0.f;
+  wp = 0.f;
   constexpr int EPW = BS / 4;  // elements per window
-  for (int w = ch.elem_begin; w < ch.elem_end; w += EPW) {
+  // window loads: connectivity, stored stress and plastic strain of this lane's point,
+  // the element's colour and the window's first and last colours
+  int ln[10];
+  float4 s4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 s2 = make_float2(0.f, 0.f);
+  float ep0 = 0.f;
+  int wcol = -1, wc0 = 0, wc1 = -1;
+  auto window_loads = [&](int w) {
     const int e = w + (tid >> 2);
     const bool act = e < ch.elem_end;
     const int ee = act ? e : ch.elem_begin;  // inactive lanes shadow a valid element
-    int ln[10];
 #pragma unroll
     for (int a = 0; a < 10; a++) ln[a] = P.conn_local[(size_t)a * E + ee];
     const size_t qi = (size_t)ee * 4 + q;
-    float4 s4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    float2 s2 = make_float2(0.f, 0.f);
-    float ep0 = 0.f;
     if (MODE == EM_J2) {
       s4 = CG ? __ldcg(A.sig_a + qi) : A.sig_a[qi];
       s2 = CG ? __ldcg(A.sig_b + qi) : A.sig_b[qi];
       ep0 = CG ? __ldcg(A.epbar + qi) : A.epbar[qi];
     }
+    wcol = act ? P.color[e] : -1;
+    wc0 = P.color[w];
+    wc1 = P.color[min(w + EPW, ch.elem_end) - 1];
+  };
+  if (PF && ch.elem_begin < ch.elem_end) window_loads(ch.elem_begin);
+  for (int w = ch.elem_begin; w < ch.elem_end; w += EPW) {
+    const int e = w + (tid >> 2);
+    const bool act = e < ch.elem_end;
+    const int ee = act ? e : ch.elem_begin;
+    const size_t qi = (size_t)ee * 4 + q;
+    if (!PF) window_loads(w);
     float2 JG[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) JG[k] = make_float2(0.f, 0.f);
@@ -1144,9 +1161,8 @@ __device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const Ele
     const int own0 = q == 0 ? ln[0] : q == 1 ? ln[1] : q == 2 ? ln[2] : ln[3];
     const int own1 = q == 0 ? ln[4] : q == 1 ? ln[5] : q == 2 ? ln[6] : ln[7];
     const int own2 = q == 0 ? ln[8] : ln[9];
-    const int col = act ? P.color[e] : -1;
-    const int c0 = P.color[w];
-    const int c1 = P.color[min(w + EPW, ch.elem_end) - 1];
+    const int col = wcol, c0 = wc0, c1 = wc1;
+    if (PF && w + EPW < ch.elem_end) window_loads(w + EPW);
     for (int k = c0; k <= c1; k++) {
       __syncthreads();
       if (col == k) {
@@ -1170,9 +1186,19 @@ __device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const Ele
       }
     }
   }
+}
+
+// The fused kernels' element phase: the loop, then the chunk's partial nodal forces to
+// the halo and its work to chunk c's sums.
+template <int MODE, int BS, bool PF>
+__device__ __forceinline__ void step_qp10_elements(const FusedArgs& A, const ElemParams& ep,
+                                                   const ChunkInfo& ch, const Tile& T, int tid,
+                                                   int c, float* red) {
+  float wint, wp;
+  qp10_element_loop<MODE, BS, false, PF>(A, ep, ch, T, tid, wint, wp);
   __syncthreads();
   node_epilogue<BS>(A, ch, T, tid);
-  if (ep.accum_energy) add_chunk_work<BS, CG>(A, c, wint, wp, red);
+  if (ep.accum_energy) add_chunk_work<BS>(A, c, wint, wp, red);
 }
 
 // 6 CTAs of 128 threads per SM (80 registers) fit the 896-node chunk's shared tile
@@ -1189,7 +1215,7 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
   stage_nodes<BS>(A, cs.ep, cs.np, ch, cs.state_final, T, threadIdx.x);
   if (cs.mode == 1) return;
   __syncthreads();
-  step_qp10_elements<MODE, BS>(A, cs.ep, ch, T, threadIdx.x, blockIdx.x, red);
+  step_qp10_elements<MODE, BS, true>(A, cs.ep, ch, T, threadIdx.x, blockIdx.x, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -1225,10 +1251,13 @@ struct FlowArgs {
   FusedArgs A[2];        // buffers of an even / odd step: state cur/prv, halo cur/prv
   float4* rec_a[2];      // per node and parity: (u_x, u_y, u_z, dt v_x) in FP32
   float2* rec_b[2];      //                       (dt v_y, dt v_z)
-  const int* own_row;    // chunks owning a local node of chunk c: own_idx[own_row[c] ..]
-  const int* own_idx;
-  const int* touch_row;  // chunks with a slot of a node chunk c owns: touch_idx[touch_row[c] ..]
-  const int* touch_idx;
+  // [2][C][desc_stride] ints, 16-byte aligned: kind 0 = element task, 1 = node task, by
+  // position in the task order of the chunks; ChunkInfo, the chunk id at kFlowDescChunk,
+  // the length of the task's dependency list at kFlowDescCount and the list from
+  // kFlowDescHead (element task: the chunks owning one of its local nodes; node task:
+  // the chunks holding a local entry of a node it owns)
+  const int* desc;
+  int desc_stride;       // a multiple of 4
   int* node_done;        // [C] last j whose N(j, c) finished (-1 before the first)
   int* elem_done;        // [C] last j whose E(j, c) finished
   int* task_ctr;
@@ -1238,6 +1267,10 @@ struct FlowArgs {
 };
 
 constexpr unsigned long long kFlowWaitNs = 2000000000ull;  // 2 s without the awaited progress
+constexpr int kFlowDescCount = 9;
+constexpr int kFlowDescChunk = 10;
+constexpr int kFlowDescHead = 12;
+static_assert(sizeof(ChunkInfo) == kFlowDescCount * sizeof(int), "descriptor header layout");
 
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
@@ -1255,16 +1288,16 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Warp 0: wait until ctr[idx[k]] >= target for every k in [b, e), lane l polling entries
-// l, l + 32, ... at once (one round trip to L2 for a typical task's 5 - 10 neighbours);
-// false on abort or timeout (the same on every lane).
-__device__ __forceinline__ bool flow_wait(const FlowArgs& F, const int* ctr, const int* idx, int b,
-                                          int e, int target) {
+// One warp: wait until ctr[dep[k]] >= target for every k < n (dep in shared memory),
+// lane l polling entries l, l + 32, ... at once (one round trip to L2 when the
+// dependencies are met); false on abort or timeout (the same on every lane).
+__device__ __forceinline__ bool flow_wait(const FlowArgs& F, const int* ctr, const int* dep, int n,
+                                          int target) {
   const int lane = threadIdx.x & 31;
   bool ok = true;
   unsigned long long t0 = 0;
-  for (int k = b + lane; k < e && ok; k += 32) {
-    const int* p = ctr + idx[k];
+  for (int k = lane; k < n && ok; k += 32) {
+    const int* p = ctr + dep[k];
     for (unsigned spins = 0; ld_acquire(p) < target; spins++) {
       if (spins >= 4) __nanosleep(128);
       if ((spins & 31u) == 31u) {
@@ -1286,11 +1319,46 @@ __device__ __forceinline__ bool flow_wait(const FlowArgs& F, const int* ctr, con
   return __all_sync(0xffffffffu, ok);
 }
 
-// Thread 0 after the CTA's writes and a barrier: publish ctr[c] = j.
-__device__ __forceinline__ void flow_publish(int* ctr, int c, int j) {
-  __threadfence();
-  st_release(ctr + c, j);
+// 16-byte asynchronous copies global -> shared (through L2), completed by cp_async_wait
+// in the issuing thread.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
 }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Task t: j (the step whose state it completes or uses), position r of its chunk in the
+// task order, element or node task.  Order: N(0, .) for every chunk, then per step j the
+// element tasks E(j, .) and the node tasks N(j + 1, .), each block in the task order of
+// the chunks.
+__device__ __forceinline__ void flow_decode(int t, int C, int& j, int& r, bool& elem) {
+  if (t < C) {
+    j = 0;
+    r = t;
+    elem = false;
+  } else {
+    const int q = (t - C) % (2 * C);
+    j = (t - C) / (2 * C);
+    elem = q < C;
+    r = elem ? q : q - C;
+    if (!elem) j++;
+  }
+}
+
+// One warp: copy task t's descriptor into buf (one commit group).
+__device__ __forceinline__ void flow_fetch(const FlowArgs& F, int t, int* buf) {
+  int j, r;
+  bool elem;
+  flow_decode(t, F.C, j, r, elem);
+  const int* src = F.desc + ((size_t)(elem ? 0 : F.C) + r) * F.desc_stride;
+  for (int k = threadIdx.x & 31; 4 * k < F.desc_stride; k += 32) cp_async16(buf + 4 * k, src + 4 * k);
+  cp_async_commit();
+}
+
+// One thread after the CTA's writes and a barrier: publish ctr[c] = j (the release
+// store orders the CTA's writes, which the barrier made visible to this thread, before it).
+__device__ __forceinline__ void flow_publish(int* ctr, int c, int j) { st_release(ctr + c, j); }
 
 // N(j, c): S^j of the nodes chunk c owns and their records.  Each thread takes KN nodes
 // at a time and issues all their loads before the first update (the node task has the
@@ -1379,82 +1447,125 @@ __device__ __forceinline__ void flow_nodes(const FlowArgs& F, const ElemParams& 
   }
 }
 
-// E(j, c): the chunk's local nodes from the records of step j into the tile.
+// E(j, c): the chunk's local nodes from the records of step j into the tile, KS nodes
+// per thread in flight (their index, record and reference-position loads issued before
+// the first shared-memory store).
 template <int BS>
 __device__ __forceinline__ void flow_stage(const FlowArgs& F, const ChunkInfo& ch, const Tile& T,
                                            int j) {
+  constexpr int KS = 4;
   const DevPlan& P = F.A[0].P;
   const float4* ra = F.rec_a[j & 1];
   const float2* rb = F.rec_b[j & 1];
-  for (int l = threadIdx.x; l < ch.n_local; l += BS) {
-    const int lb = ch.local_begin + l;
-    const int g = l < ch.n_own ? ch.own_begin + l : P.local_gid[lb];
-    const float4 r0 = __ldcg(ra + g);
-    const float2 r1 = __ldcg(rb + g);
-    float x0[3];
+  for (int l0 = threadIdx.x; l0 < ch.n_local; l0 += KS * BS) {
+    int lb[KS], g[KS];
 #pragma unroll
-    for (int k = 0; k < 3; k++) x0[k] = P.local_x0[k * (size_t)P.Lt + lb];
-    store_record(T, l, x0[0] + r0.x, x0[1] + r0.y, x0[2] + r0.z, r0.w, r1.x, r1.y);
-    T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int q = 0; q < KS; q++) {
+      const int l = min(l0 + q * BS, ch.n_local - 1);
+      lb[q] = ch.local_begin + l;
+      g[q] = l < ch.n_own ? ch.own_begin + l : P.local_gid[lb[q]];
+    }
+    float4 r0[KS];
+    float2 r1[KS];
+    float x0[KS][3];
+#pragma unroll
+    for (int q = 0; q < KS; q++) {
+      r0[q] = __ldcg(ra + g[q]);
+      r1[q] = __ldcg(rb + g[q]);
+#pragma unroll
+      for (int k = 0; k < 3; k++) x0[q][k] = P.local_x0[k * (size_t)P.Lt + lb[q]];
+    }
+#pragma unroll
+    for (int q = 0; q < KS; q++) {
+      const int l = l0 + q * BS;
+      if (l < ch.n_local) {
+        store_record(T, l, x0[q][0] + r0[q].x, x0[q][1] + r0[q].y, x0[q][2] + r0[q].z, r0[q].w,
+                     r1[q].x, r1[q].y);
+        T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
   }
 }
 
+// The persistent task kernel.  Tasks are claimed from one counter in task order, one
+// ahead of the running one.  Before task t runs, warp 0 moves t's descriptor (copied
+// into shared memory while the previous task ran) into place, claims the next task and
+// polls t's dependencies' progress counters -- one round trip for both when the
+// dependencies are met -- and starts copying the next task's descriptor (cp.async),
+// which lands while t runs; after t, a thread of the last warp publishes while warp 0
+// already polls for the next task.  A task waits only for tasks earlier in the order,
+// and the earliest unfinished claimed task is always some CTA's current one, so holding
+// a claimed task cannot deadlock; all CTAs are resident (one round of the grid).  The
+// loop keeps no counter: only shared memory carries state from one task to the next,
+// which leaves the element loop all 80 registers.
 template <int MODE, int BS>
 __global__ void __launch_bounds__(BS, 768 / BS) k_flow_qp10(FlowArgs F, ElemParams ep,
                                                           NodeParams np) {
   extern __shared__ float sm[];
   __shared__ float red[BS / 32];
-  __shared__ int sh_task, sh_next, sh_ok;
-  const int C = F.C;
-  const long long ntasks = (long long)C + 2LL * C * F.nsteps;
-  // the next task is claimed while the current one runs (one atomic round trip hidden);
-  // a claimed task waits only for tasks earlier in the claim order, so holding it is safe
+  __shared__ int sh_cur, sh_next, sh_ok;
+  int* const dcur = reinterpret_cast<int*>(sm);      // the running task's descriptor
+  int* const dnext = dcur + F.desc_stride;            // the next one's, arriving
+  const bool w0 = threadIdx.x < 32;
   if (threadIdx.x == 0) sh_next = atomicAdd(F.task_ctr, 1);
+  __syncthreads();
+  if (w0 && sh_next < F.C + 2 * F.C * F.nsteps) flow_fetch(F, sh_next, dnext);
   for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      sh_task = *(volatile int*)F.abort_flag ? -1 : sh_next;
-      if (sh_task >= 0 && sh_task < ntasks) sh_next = atomicAdd(F.task_ctr, 1);
+    if (w0) {
+      const int ntasks = F.C + 2 * F.C * F.nsteps;
+      const int t = sh_next;
+      cp_async_wait();  // t's descriptor (copied by this warp)
+      __syncwarp();
+      for (int k = threadIdx.x; k < F.desc_stride; k += 32) dcur[k] = dnext[k];
+      __syncwarp();
+      bool ok = true;
+      int tn = ntasks;
+      if (t < ntasks) {
+        int j, r;
+        bool elem;
+        flow_decode(t, F.C, j, r, elem);
+        if (threadIdx.x == 0) tn = atomicAdd(F.task_ctr, 1);
+        ok = elem ? flow_wait(F, F.node_done, dcur + kFlowDescHead, dcur[kFlowDescCount], j)
+                  : (j == 0 || flow_wait(F, F.elem_done, dcur + kFlowDescHead,
+                                         dcur[kFlowDescCount], j - 1));
+        tn = __shfl_sync(0xffffffffu, tn, 0);
+        if (ok && tn < ntasks) flow_fetch(F, tn, dnext);
+      }
+      if (threadIdx.x == 0) {
+        sh_cur = t;
+        sh_ok = ok;
+        sh_next = tn;
+      }
     }
     __syncthreads();
-    const int t = sh_task;
-    if (t < 0 || t >= ntasks) break;
-    int j, c;
+    const int t = sh_cur;
+    if (t >= F.C + 2 * F.C * F.nsteps || !sh_ok) break;
+    int j, r;
     bool elem;
-    if (t < C) {
-      j = 0;
-      c = t;
-      elem = false;
-    } else {
-      const int r = (t - C) % (2 * C);
-      j = (t - C) / (2 * C);
-      elem = r < C;
-      c = elem ? r : r - C;
-      if (!elem) j++;
-    }
-    const DevPlan& P = F.A[0].P;
-    const ChunkInfo ch = P.chunks[c];
-    if (threadIdx.x < 32) {
-      const bool ok = elem ? flow_wait(F, F.node_done, F.own_idx, F.own_row[c], F.own_row[c + 1], j)
-                           : (j == 0 || flow_wait(F, F.elem_done, F.touch_idx, F.touch_row[c],
-                                                  F.touch_row[c + 1], j - 1));
-      if (threadIdx.x == 0) sh_ok = ok;
-    }
-    __syncthreads();
-    if (!sh_ok) break;
+    flow_decode(t, F.C, j, r, elem);
+    // the descriptor is read here only: after the task's last barrier warp 0 overwrites
+    // it with the next task's
+    ChunkInfo ch;
+    memcpy(&ch, dcur, sizeof(ChunkInfo));
+    const int c = dcur[kFlowDescChunk];
     if (elem) {
-      const Tile T = make_tile(sm, ch.n_local);
+      const Tile T = make_tile(sm + 2 * F.desc_stride, ch.n_local);
       flow_stage<BS>(F, ch, T, j);
       __syncthreads();
-      step_qp10_elements<MODE, BS, true>(F.A[j & 1], ep, ch, T, threadIdx.x, c, red);
+      float wint, wp;
+      qp10_element_loop<MODE, BS, true, false>(F.A[0], ep, ch, T, threadIdx.x, wint, wp);
       __syncthreads();
-      if (threadIdx.x == 0) flow_publish(F.elem_done, c, j);
+      node_epilogue<BS>(F.A[j & 1], ch, T, threadIdx.x);
+      if (ep.accum_energy) add_chunk_work<BS, true>(F.A[0], c, wint, wp, red);
+      __syncthreads();
+      if (threadIdx.x == BS - 32) flow_publish(F.elem_done, c, j);
     } else {
       flow_nodes<BS>(F, ep, np, ch, j);
       __syncthreads();
-      if (threadIdx.x == 0) flow_publish(F.node_done, c, j);
+      if (threadIdx.x == BS - 32) flow_publish(F.node_done, c, j);
     }
   }
+  if (w0) cp_async_wait();
 }
 
 // ---------------------------------------------------------------------------

@@ -249,6 +249,109 @@ bool build_plan(int N, int E, int npe, const double* xloc, const int* conn, int 
   return true;
 }
 
+int flow_lists(const Plan& P, std::vector<int>* own_row, std::vector<int>* own_idx,
+               std::vector<int>* touch_row, std::vector<int>* touch_idx) {
+  const int C = P.n_chunks;
+  std::vector<int> owner(P.N, -1);
+  for (int c = 0; c < C; c++)
+    for (int l = 0; l < P.chunks[c].n_own; l++) owner[P.chunks[c].own_begin + l] = c;
+  std::vector<std::vector<int>> own(C), touch(C);
+  for (int c = 0; c < C; c++) {
+    const ChunkInfo& ch = P.chunks[c];
+    for (int l = 0; l < ch.n_local; l++) {
+      const int g = l < ch.n_own ? ch.own_begin + l : P.local_gid[ch.local_begin + l];
+      own[c].push_back(owner[g]);
+      touch[owner[g]].push_back(c);
+    }
+  }
+  int longest = 0;
+  auto csr = [&longest](std::vector<std::vector<int>>& lists, std::vector<int>* row,
+                        std::vector<int>* idx) {
+    row->assign(1, 0);
+    idx->clear();
+    for (auto& v : lists) {
+      std::sort(v.begin(), v.end());
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+      longest = std::max(longest, (int)v.size());
+      idx->insert(idx->end(), v.begin(), v.end());
+      row->push_back((int)idx->size());
+    }
+  };
+  csr(own, own_row, own_idx);
+  csr(touch, touch_row, touch_idx);
+  return longest;
+}
+
+std::vector<int> flow_order(int C, const std::vector<int>& own_row, const std::vector<int>& own_idx) {
+  // symmetric adjacency without self loops
+  std::vector<std::vector<int>> adj(C);
+  for (int c = 0; c < C; c++)
+    for (int k = own_row[c]; k < own_row[c + 1]; k++) {
+      const int o = own_idx[k];
+      if (o == c) continue;
+      adj[c].push_back(o);
+      adj[o].push_back(c);
+    }
+  for (auto& v : adj) {
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+  }
+  auto by_degree = [&adj](int a, int b) {
+    return adj[a].size() != adj[b].size() ? adj[a].size() < adj[b].size() : a < b;
+  };
+  for (auto& v : adj) std::sort(v.begin(), v.end(), by_degree);
+  std::vector<int> level(C, -1), order;
+  order.reserve(C);
+  std::vector<int> seen(C, 0), bfs;
+  // breadth-first levels from s within its component; returns the last level's nodes
+  auto levels = [&](int s, std::vector<int>* comp) {
+    comp->assign(1, s);
+    level[s] = 0;
+    for (size_t h = 0; h < comp->size(); h++) {
+      const int u = (*comp)[h];
+      for (int w : adj[u])
+        if (level[w] < 0) {
+          level[w] = level[u] + 1;
+          comp->push_back(w);
+        }
+    }
+    const int last = level[comp->back()];
+    std::vector<int> far;
+    for (int u : *comp) {
+      if (level[u] == last) far.push_back(u);
+      level[u] = -1;
+    }
+    return std::make_pair(last, far);
+  };
+  std::vector<int> comp;
+  for (int c0 = 0; c0 < C; c0++) {
+    if (seen[c0]) continue;
+    // pseudo-peripheral start (George and Liu): move to a lowest-degree node of the
+    // farthest level while the eccentricity grows
+    int s = c0;
+    auto lv = levels(s, &comp);
+    for (int it = 0; it < 8; it++) {
+      const int cand = *std::min_element(lv.second.begin(), lv.second.end(), by_degree);
+      auto lv2 = levels(cand, &comp);
+      if (lv2.first <= lv.first) break;
+      s = cand;
+      lv = lv2;
+    }
+    // Cuthill-McKee from s
+    const size_t begin = order.size();
+    order.push_back(s);
+    seen[s] = 1;
+    for (size_t h = begin; h < order.size(); h++)
+      for (int w : adj[order[h]])
+        if (!seen[w]) {
+          seen[w] = 1;
+          order.push_back(w);
+        }
+    std::reverse(order.begin() + begin, order.end());
+  }
+  return order;
+}
+
 bool verify_plan(const Plan& P, const int* conn, std::string* err) {
   const int E = P.E, N = P.N, npe = P.npe;
   std::vector<int> seen(E, 0);

@@ -62,6 +62,20 @@ constexpr int kDefaultTargetCtas = 608;
 bool build_plan(int N, int E, int npe, const double* xloc, const int* conn, int chunk_elements,
                 int chunk_nodes, int target_ctas, Plan* plan, std::string* err);
 
+// Dependency lists of the task kernel, CSR by chunk, each list sorted and unique:
+// own[c] = the chunks owning one of chunk c's local nodes (its element tasks read their
+// node records), touch[c] = the chunks holding a local entry of a node chunk c owns
+// (its node tasks sum their partial forces).  Returns the longest list.
+int flow_lists(const Plan& P, std::vector<int>* own_row, std::vector<int>* own_idx,
+               std::vector<int>* touch_row, std::vector<int>* touch_idx);
+
+// Task order of the chunks for the task kernel: reverse Cuthill-McKee on the graph of
+// chunks sharing a node (the own lists, made symmetric), components in order of their
+// lowest chunk, each from a pseudo-peripheral chunk, neighbours by degree then id.
+// Chunks that share nodes get nearby positions, so every task's dependencies lie about
+// one block of C tasks back in the claim order.
+std::vector<int> flow_order(int C, const std::vector<int>& own_row, const std::vector<int>& own_idx);
+
 // Host check of the plan invariants (used by tests through ci_plan_verify).
 bool verify_plan(const Plan& p, const int* conn, std::string* err);
 

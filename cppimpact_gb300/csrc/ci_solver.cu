@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -124,9 +125,9 @@ struct ci_solver {
   // and the abort flag ([2C + 2] ints), and the CTAs it keeps resident
   DBuf<float4> d_rec_a[2];
   DBuf<float2> d_rec_b[2];
-  DBuf<int> d_own_row, d_own_idx, d_touch_row, d_touch_idx, d_flow_ctr;
-  int flow_ctas = 0;
-  std::vector<int> own_row, own_idx, touch_row, touch_idx;  // host copies
+  DBuf<int> d_flow_desc, d_flow_ctr;
+  int flow_ctas = 0, flow_stride = 0;
+  size_t flow_smem = 0;
   bool xc_stale = true;  // X changed since d_Xc was uploaded
   // nodal strain/stress output: last element (caller order) of every node, and the plan
   // position of every caller element (built on first use)
@@ -269,14 +270,6 @@ cudaError_t configure_step(int bytes) {
     if ((e = cudaFuncSetAttribute(ci::k_step_qp10<ci::EM_REFCOMPAT, BS>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
       return e;
-    if (BS == 128) {
-      if ((e = cudaFuncSetAttribute(ci::k_flow_qp10<ci::EM_J2, 128>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-        return e;
-      if ((e = cudaFuncSetAttribute(ci::k_flow_qp10<ci::EM_REFCOMPAT, 128>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-        return e;
-    }
   }
   return cudaFuncSetAttribute(ci::k_step<NPE, ci::EM_REFCOMPAT, BS>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -536,59 +529,54 @@ int build_graph(ci_solver* s, int steps) {
 template <typename T>
 int upload(DBuf<T>& b, const std::vector<T>& h, cudaStream_t st);
 
-// Task kernel (step_kernel = 2): for every chunk the chunks owning one of its local
-// nodes (whose node tasks its element task waits for) and the chunks holding a slot of
-// a node it owns (whose element tasks its node task waits for), as CSR lists; record
-// buffers, counters and the number of CTAs kept resident.
+// Task kernel (step_kernel = 2): one descriptor per (task kind, position in the task
+// order of the chunks) -- the chunk's ChunkInfo, its id, the length of its dependency
+// list and the list (the chunks owning one of its local nodes for the element task, the
+// chunks holding a local entry of a node it owns for the node task) in a fixed stride,
+// so that a CTA copies the next task's descriptor into shared memory in one round trip;
+// record buffers, counters and the number of CTAs kept resident.
 int setup_flow(ci_solver* s) {
   const ci::Plan& P = s->plan;
   const int C = s->C;
-  std::vector<int> owner(s->N, -1);
-  for (int c = 0; c < C; c++)
-    for (int l = 0; l < P.chunks[c].n_own; l++) owner[P.chunks[c].own_begin + l] = c;
-  std::vector<std::vector<int>> own(C), touch(C);
-  for (int c = 0; c < C; c++) {
-    const ci::ChunkInfo& ch = P.chunks[c];
-    for (int l = 0; l < ch.n_local; l++) {
-      const int g = l < ch.n_own ? ch.own_begin + l : P.local_gid[ch.local_begin + l];
-      own[c].push_back(owner[g]);
-      touch[owner[g]].push_back(c);
+  std::vector<int> own_row, own_idx, touch_row, touch_idx;
+  const int longest = ci::flow_lists(P, &own_row, &own_idx, &touch_row, &touch_idx);
+  const std::vector<int> order = ci::flow_order(C, own_row, own_idx);
+  if ((int)order.size() != C) return fail(CI_ERR_INVALID, "task order of %d chunks has %zu", C, order.size());
+  const int stride = ci::kFlowDescHead + ((longest + 3) & ~3);
+  std::vector<int> desc(2 * (size_t)C * stride, 0);
+  for (int kind = 0; kind < 2; kind++)
+    for (int r = 0; r < C; r++) {
+      const int c = order[r];
+      int* d = desc.data() + ((size_t)kind * C + r) * stride;
+      std::memcpy(d, &P.chunks[c], sizeof(ci::ChunkInfo));
+      const std::vector<int>& row = kind == 0 ? own_row : touch_row;
+      const std::vector<int>& idx = kind == 0 ? own_idx : touch_idx;
+      d[ci::kFlowDescChunk] = c;
+      d[ci::kFlowDescCount] = row[c + 1] - row[c];
+      std::copy(idx.begin() + row[c], idx.begin() + row[c + 1], d + ci::kFlowDescHead);
     }
-  }
-  auto csr = [](std::vector<std::vector<int>>& lists, std::vector<int>* row, std::vector<int>* idx) {
-    row->assign(1, 0);
-    idx->clear();
-    for (auto& v : lists) {
-      std::sort(v.begin(), v.end());
-      v.erase(std::unique(v.begin(), v.end()), v.end());
-      idx->insert(idx->end(), v.begin(), v.end());
-      row->push_back((int)idx->size());
-    }
-  };
-  csr(own, &s->own_row, &s->own_idx);
-  csr(touch, &s->touch_row, &s->touch_idx);
+  s->flow_stride = stride;
+  s->flow_smem = s->smem_bytes + 2 * sizeof(int) * (size_t)stride;
   int rc;
-  if ((rc = upload(s->d_own_row, s->own_row, s->stream))) return rc;
-  if ((rc = upload(s->d_own_idx, s->own_idx, s->stream))) return rc;
-  if ((rc = upload(s->d_touch_row, s->touch_row, s->stream))) return rc;
-  if ((rc = upload(s->d_touch_idx, s->touch_idx, s->stream))) return rc;
+  if ((rc = upload(s->d_flow_desc, desc, s->stream))) return rc;
   for (int p = 0; p < 2; p++) {
     CI_CUDA(s->d_rec_a[p].alloc(s->N));
     CI_CUDA(s->d_rec_b[p].alloc(s->N));
   }
   CI_CUDA(s->d_flow_ctr.alloc(2 * (size_t)C + 2));
+  auto kern = s->opt.mode != CI_MODE_REFCOMPAT ? ci::k_flow_qp10<ci::EM_J2, 128>
+                                               : ci::k_flow_qp10<ci::EM_REFCOMPAT, 128>;
+  CI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->flow_smem));
   int per_sm = 0, sms = 0;
-  CI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, s->opt.mode != CI_MODE_REFCOMPAT ? ci::k_flow_qp10<ci::EM_J2, 128>
-                                                : ci::k_flow_qp10<ci::EM_REFCOMPAT, 128>,
-      128, s->smem_bytes));
+  CI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, s->flow_smem));
   CI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
   s->flow_ctas = std::max(1, std::min(per_sm * sms, C));
   return CI_OK;
 }
 
-// n steps in launches of the task kernel (at most kFlowMaxSteps steps each, so the task
-// count fits an int), each from a complete state in buffer A to a complete state in A.
+// n steps in launches of the task kernel (at most kFlowMaxSteps steps each, and few
+// enough that the task count C (2 k + 1) fits an int), each from a complete state in
+// buffer A to a complete state in A.
 constexpr int kFlowMaxSteps = 1 << 16;
 
 cudaError_t enqueue_flow(ci_solver* s, int n) {
@@ -596,7 +584,7 @@ cudaError_t enqueue_flow(ci_solver* s, int n) {
   const ci::ElemParams ep = s->elem_params((float)s->dt, true);
   const ci::NodeParams np = s->node_params();
   for (int done = 0; done < n;) {
-    const int k = std::min(n - done, kFlowMaxSteps);
+    const int k = std::min({n - done, kFlowMaxSteps, (INT_MAX - C) / (2 * C)});
     ci::FlowArgs F;
     F.A[0] = s->fused_args(true, 0, false, false);
     F.A[1] = s->fused_args(false, 1, false, false);
@@ -604,10 +592,8 @@ cudaError_t enqueue_flow(ci_solver* s, int n) {
       F.rec_a[p] = s->d_rec_a[p].p;
       F.rec_b[p] = s->d_rec_b[p].p;
     }
-    F.own_row = s->d_own_row.p;
-    F.own_idx = s->d_own_idx.p;
-    F.touch_row = s->d_touch_row.p;
-    F.touch_idx = s->d_touch_idx.p;
+    F.desc = s->d_flow_desc.p;
+    F.desc_stride = s->flow_stride;
     F.node_done = s->d_flow_ctr.p;
     F.elem_done = s->d_flow_ctr.p + C;
     F.task_ctr = s->d_flow_ctr.p + 2 * C;
@@ -619,9 +605,9 @@ cudaError_t enqueue_flow(ci_solver* s, int n) {
     if ((e = cudaMemsetAsync(s->d_flow_ctr.p, 0xff, sizeof(int) * 2 * (size_t)C, s->stream))) return e;
     if ((e = cudaMemsetAsync(F.task_ctr, 0, 2 * sizeof(int), s->stream))) return e;
     if (s->opt.mode != CI_MODE_REFCOMPAT)
-      ci::k_flow_qp10<ci::EM_J2, 128><<<s->flow_ctas, 128, s->smem_bytes, s->stream>>>(F, ep, np);
+      ci::k_flow_qp10<ci::EM_J2, 128><<<s->flow_ctas, 128, s->flow_smem, s->stream>>>(F, ep, np);
     else
-      ci::k_flow_qp10<ci::EM_REFCOMPAT, 128><<<s->flow_ctas, 128, s->smem_bytes, s->stream>>>(F, ep, np);
+      ci::k_flow_qp10<ci::EM_REFCOMPAT, 128><<<s->flow_ctas, 128, s->flow_smem, s->stream>>>(F, ep, np);
     if ((e = cudaGetLastError())) return e;
     if (k & 1) {
       const size_t b = sizeof(double) * 3 * (size_t)s->N;
@@ -1651,7 +1637,8 @@ int ci_plan_stats(const ci_mesh* mesh, int chunk_elements, int chunk_nodes, long
   stats[4] = P.max_chunk_elems;
   stats[5] = P.n_ghosts;
   stats[6] = P.n_boundary;
-  stats[7] = 0;
+  std::vector<int> r0, i0, r1, i1;
+  stats[7] = ci::flow_lists(P, &r0, &i0, &r1, &i1);
   if (perm_elems) std::memcpy(perm_elems, P.elem_orig.data(), sizeof(int) * P.E);
   if (perm_nodes) std::memcpy(perm_nodes, P.node_orig.data(), sizeof(int) * P.N);
   return CI_OK;

@@ -339,7 +339,8 @@ void ci_mesh_free(ci_mesh* m);
 /* Preprocessing summary (host only, no GPU needed): space-filling-curve order,
  * chunking, node ownership and per-chunk colouring.  stats[0..7] = chunks,
  * max colours, max local nodes, total slots, max chunk elements, ghosts, boundary
- * nodes, 0. perm_elems (may be NULL, [E]) receives the plan order of elements
+ * nodes, the longest dependency list of the task kernel (chunks a chunk's element task
+ * or node task waits for). perm_elems (may be NULL, [E]) receives the plan order of elements
  * (original ids), perm_nodes (may be NULL, [N]) the plan order of nodes. */
 int ci_plan_stats(const ci_mesh* mesh, int chunk_elements, int chunk_nodes, long long* stats,
                   int* perm_elems, int* perm_nodes);

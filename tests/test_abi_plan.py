@@ -68,6 +68,9 @@ def test_plan_shell_workload_shape(cilib):
     st = cilib.plan_stats(s.xloc, s.conn)
     assert st["max_local"] <= 896             # default local-node budget per chunk
     assert st["ghosts"] < 0.30 * s.num_nodes
+    # each task of the task kernel waits for a handful of neighbouring chunks (its
+    # descriptor holds the list: 4 bytes per entry of shared memory, twice)
+    assert 2 <= st["max_task_deps"] <= 32
 
 
 def test_plan_rejects_bad_meshes(cilib):

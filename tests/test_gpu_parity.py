@@ -392,6 +392,30 @@ def test_task_kernel_bitwise_equal_to_fused(cilib, mesh, mode, speed, calls):
     assert ea["internal"] == eb["internal"] and ea["kinetic"] == eb["kinetic"]
 
 
+def test_task_kernel_long_launch_on_the_shell(cilib):
+    """The full shell (1,736 chunks, 912 resident CTAs) for 2,000 steps in one launch of
+    the task kernel -- 6.9 million tasks, each CTA moving through thousands of task
+    descriptors -- ends bit for bit where the fused kernel does.  A task that waited past
+    its time limit would raise here."""
+    m = mg.shell()
+    setup = mg.impact_setup(m, 5.0, 0.0)
+    out = []
+    for sk in (3, 2):
+        s = solver(cilib, m, cilib.MODE_J2, wall_normal=setup["wall_normal"],
+                   wall_offset=setup["wall_offset"], wall_stiffness=setup["wall_stiffness"],
+                   step_kernel=sk)
+        assert s.step_kernel() == sk
+        s.initialize(setup["vel"])
+        s.start(setup["dt"])
+        s.step(2000)
+        out.append(s.state(("x", "v", "contact")))
+        s.close()
+    a, b = out
+    assert ((a["contact"] & 2) > 0).sum() > 0, "the run must reach the plane"
+    for k in ("x", "v", "contact"):
+        assert np.array_equal(a[k], b[k]), k
+
+
 def test_task_kernel_rejects_other_element_types(cilib):
     m = mg.cube(3, 1)
     with pytest.raises(cilib.CiError) as e:
