@@ -641,6 +641,15 @@ __device__ __forceinline__ void load_pairs(const Tile& T, int l, float2 (&p)[3])
   p[2] = T.p1[l];
 }
 
+// Zero local node l's force accumulator and keep the node's halo slot in this chunk in
+// its fourth lane (as int bits; the element loops add to x, y, z only), so that the
+// epilogue writes the partial forces without a dependent load.
+__device__ __forceinline__ void init_acc(const Tile& T, const ChunkInfo& ch, const DevPlan& P,
+                                         int l) {
+  const int s = l < ch.n_int ? ch.slot_begin + l : P.local_slot[ch.local_begin + l];
+  T.acc[l] = make_float4(0.f, 0.f, 0.f, __int_as_float(s));
+}
+
 __device__ __forceinline__ Tile make_tile(float* sm, int L) {
   Tile t;
   t.p0 = reinterpret_cast<float4*>(sm);
@@ -710,7 +719,7 @@ __device__ __forceinline__ void stage_nodes(const FusedArgs& A, const ElemParams
     }
     store_record(T, l, x0[0] + uf[0], x0[1] + uf[1], x0[2] + uf[2], ep.dt * vf[0], ep.dt * vf[1],
                  ep.dt * vf[2]);
-    T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+    init_acc(T, ch, P, l);
   }
 }
 
@@ -780,38 +789,40 @@ __device__ __forceinline__ void stage_nodes_k(const FusedArgs& A, const ElemPara
       if (l < ch.n_own) store_node(A, A.u_cur, A.v_cur, g[j], u[j], v[j], vf, a, hit, false, ct[j]);
       store_record(T, l, x0[j][0] + uf[0], x0[j][1] + uf[1], x0[j][2] + uf[2], ep.dt * vf[0],
                    ep.dt * vf[1], ep.dt * vf[2]);
-      T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+      init_acc(T, ch, P, l);
     }
   }
 }
 
-// Every local node's partial force of this step to its slot in the halo.
+// Every local node's partial force of this step to its slot in the halo (the slot kept in
+// the accumulator's fourth lane by init_acc).
 template <int BS>
 __device__ __forceinline__ void node_epilogue(const FusedArgs& A, const ChunkInfo& ch,
                                               const Tile& T, int tid) {
-  const DevPlan& P = A.P;
   const int L = ch.n_local;
 #pragma unroll 4
   for (int l = tid; l < L; l += BS) {
     const float4 f = T.acc[l];
-    const int s = l < ch.n_int ? ch.slot_begin + l : P.local_slot[ch.local_begin + l];
+    const int s = __float_as_int(f.w);
     A.halo_cur[0][s] = f.x;
     A.halo_cur[1][s] = f.y;
     A.halo_cur[2][s] = f.z;
   }
 }
 
-// The CTA's internal and plastic work of this step added to chunk c's running sums
-// (CG: read them through L2 only, for kernels in which another SM wrote them last).
-template <int BS, bool CG = false>
+// The CTA's internal and plastic work of this step added to chunk c's running sums by
+// reductions at L2 (no round trip before the CTA's next barrier).  Only one CTA at a time
+// updates a chunk's sums, in step order, so every addition is the one
+// sums = sums + (double)t of the step order, and the sums' bits do not depend on timing.
+template <int BS>
 __device__ __forceinline__ void add_chunk_work(const FusedArgs& A, int c, float wint, float wp,
                                                float* red) {
   const float t0 = block_sum<BS>(wint, red);
   const float t1 = block_sum<BS>(wp, red);
   if (threadIdx.x == 0) {
     double* cw = A.chunk_work + 4 * (size_t)c;
-    cw[0] = (CG ? __ldcg(cw) : cw[0]) + (double)t0;
-    cw[1] = (CG ? __ldcg(cw + 1) : cw[1]) + (double)t1;
+    atomicAdd(cw, (double)t0);
+    atomicAdd(cw + 1, (double)t1);
   }
 }
 
@@ -1453,17 +1464,18 @@ __device__ __forceinline__ void flow_nodes(const FlowArgs& F, const ElemParams& 
 template <int BS>
 __device__ __forceinline__ void flow_stage(const FlowArgs& F, const ChunkInfo& ch, const Tile& T,
                                            int j) {
-  constexpr int KS = 4;
+  constexpr int KS = 2;
   const DevPlan& P = F.A[0].P;
   const float4* ra = F.rec_a[j & 1];
   const float2* rb = F.rec_b[j & 1];
   for (int l0 = threadIdx.x; l0 < ch.n_local; l0 += KS * BS) {
-    int lb[KS], g[KS];
+    int lb[KS], g[KS], sl[KS];
 #pragma unroll
     for (int q = 0; q < KS; q++) {
       const int l = min(l0 + q * BS, ch.n_local - 1);
       lb[q] = ch.local_begin + l;
       g[q] = l < ch.n_own ? ch.own_begin + l : P.local_gid[lb[q]];
+      sl[q] = l < ch.n_int ? ch.slot_begin + l : P.local_slot[lb[q]];
     }
     float4 r0[KS];
     float2 r1[KS];
@@ -1481,7 +1493,7 @@ __device__ __forceinline__ void flow_stage(const FlowArgs& F, const ChunkInfo& c
       if (l < ch.n_local) {
         store_record(T, l, x0[q][0] + r0[q].x, x0[q][1] + r0[q].y, x0[q][2] + r0[q].z, r0[q].w,
                      r1[q].x, r1[q].y);
-        T.acc[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+        T.acc[l] = make_float4(0.f, 0.f, 0.f, __int_as_float(sl[q]));
       }
     }
   }
@@ -1556,7 +1568,7 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_flow_qp10(FlowArgs F, ElemPara
       qp10_element_loop<MODE, BS, true, false>(F.A[0], ep, ch, T, threadIdx.x, wint, wp);
       __syncthreads();
       node_epilogue<BS>(F.A[j & 1], ch, T, threadIdx.x);
-      if (ep.accum_energy) add_chunk_work<BS, true>(F.A[0], c, wint, wp, red);
+      if (ep.accum_energy) add_chunk_work<BS>(F.A[0], c, wint, wp, red);
       __syncthreads();
       if (threadIdx.x == BS - 32) flow_publish(F.elem_done, c, j);
     } else {
