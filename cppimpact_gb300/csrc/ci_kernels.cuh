@@ -1371,14 +1371,14 @@ __device__ __forceinline__ void flow_fetch(const FlowArgs& F, int t, int* buf) {
 // store orders the CTA's writes, which the barrier made visible to this thread, before it).
 __device__ __forceinline__ void flow_publish(int* ctr, int c, int j) { st_release(ctr + c, j); }
 
-// N(j, c): S^j of the nodes chunk c owns and their records.  Each thread takes KN nodes
-// at a time and issues all their loads before the first update (the node task has the
-// registers the element task needs to spare); every node's arithmetic is the fused
-// kernel's staging.
+// N(j, c): S^j of the nodes chunk c owns and their records, one node per thread at a
+// time (two in flight leave the element loop of the same kernel too few registers for
+// its window prefetch, which gains more); every node's arithmetic is the fused kernel's
+// staging.
 template <int BS>
 __device__ __forceinline__ void flow_nodes(const FlowArgs& F, const ElemParams& ep,
                                            const NodeParams& np, const ChunkInfo& ch, int j) {
-  constexpr int KN = 2;
+  constexpr int KN = 1;
   const FusedArgs& A = F.A[j & 1];
   const DevPlan& P = A.P;
   float4* ra = F.rec_a[j & 1];
@@ -1565,7 +1565,7 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_flow_qp10(FlowArgs F, ElemPara
       flow_stage<BS>(F, ch, T, j);
       __syncthreads();
       float wint, wp;
-      qp10_element_loop<MODE, BS, true, false>(F.A[0], ep, ch, T, threadIdx.x, wint, wp);
+      qp10_element_loop<MODE, BS, true, true>(F.A[0], ep, ch, T, threadIdx.x, wint, wp);
       __syncthreads();
       node_epilogue<BS>(F.A[j & 1], ch, T, threadIdx.x);
       if (ep.accum_energy) add_chunk_work<BS>(F.A[0], c, wint, wp, red);
