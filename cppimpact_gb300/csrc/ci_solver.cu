@@ -123,8 +123,7 @@ struct ci_solver {
   // persistent task kernel (step_kernel = 2): node records of the two parities, the
   // owner / toucher lists of every chunk, per-chunk progress counters, the task counter
   // and the abort flag ([2C + 2] ints), and the CTAs it keeps resident
-  DBuf<float4> d_rec_a[2];
-  DBuf<float2> d_rec_b[2];
+  DBuf<float4> d_rec;  // task kernel records: [2][N] float4 then [2][N] float2
   DBuf<int> d_flow_desc, d_flow_ctr;
   int flow_ctas = 0, flow_stride = 0;
   size_t flow_smem = 0;
@@ -559,9 +558,26 @@ int setup_flow(ci_solver* s) {
   s->flow_smem = s->smem_bytes + 2 * sizeof(int) * (size_t)stride;
   int rc;
   if ((rc = upload(s->d_flow_desc, desc, s->stream))) return rc;
-  for (int p = 0; p < 2; p++) {
-    CI_CUDA(s->d_rec_a[p].alloc(s->N));
-    CI_CUDA(s->d_rec_b[p].alloc(s->N));
+  CI_CUDA(s->d_rec.alloc(3 * (size_t)s->N));
+  {
+    // the records go from a node task to the element tasks of the same step: keep them
+    // in L2 (a persisting access window over the one allocation)
+    int max_persist = 0, max_window = 0;
+    CI_CUDA(cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, s->device));
+    CI_CUDA(cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, s->device));
+    const size_t bytes = sizeof(float4) * 3 * (size_t)s->N;
+    if (max_persist > 0 && max_window > 0) {
+      const size_t limit = std::min(bytes, (size_t)max_persist);
+      CI_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, limit));
+      cudaStreamAttrValue attr = {};
+      attr.accessPolicyWindow.base_ptr = s->d_rec.p;
+      attr.accessPolicyWindow.num_bytes = std::min(bytes, (size_t)max_window);
+      attr.accessPolicyWindow.hitRatio =
+          (float)std::min(1.0, (double)limit / (double)attr.accessPolicyWindow.num_bytes);
+      attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+      attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+      CI_CUDA(cudaStreamSetAttribute(s->stream, cudaStreamAttributeAccessPolicyWindow, &attr));
+    }
   }
   CI_CUDA(s->d_flow_ctr.alloc(2 * (size_t)C + 2));
   auto kern = s->opt.mode != CI_MODE_REFCOMPAT ? ci::k_flow_qp10<ci::EM_J2, 128>
@@ -589,8 +605,8 @@ cudaError_t enqueue_flow(ci_solver* s, int n) {
     F.A[0] = s->fused_args(true, 0, false, false);
     F.A[1] = s->fused_args(false, 1, false, false);
     for (int p = 0; p < 2; p++) {
-      F.rec_a[p] = s->d_rec_a[p].p;
-      F.rec_b[p] = s->d_rec_b[p].p;
+      F.rec_a[p] = s->d_rec.p + (size_t)p * s->N;
+      F.rec_b[p] = reinterpret_cast<float2*>(s->d_rec.p + 2 * (size_t)s->N) + (size_t)p * s->N;
     }
     F.desc = s->d_flow_desc.p;
     F.desc_stride = s->flow_stride;
