@@ -101,6 +101,7 @@ EXPORTS = {
     "ci_time_kernels": (C.c_int, [C.c_void_p, C.c_int, _fp]),
     "ci_launches_per_step": (C.c_int, [C.c_void_p]),
     "ci_step_kernel": (C.c_int, [C.c_void_p]),
+    "ci_debug_flow_stall": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "ci_mesh_load_inp": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(CiMesh)]),
     "ci_mesh_free": (None, [C.POINTER(CiMesh)]),
     "ci_plan_stats": (C.c_int, [C.POINTER(CiMesh), C.c_int, C.c_int, C.POINTER(C.c_longlong),
@@ -359,6 +360,11 @@ class Solver:
         """The step kernel this solver runs: 1 element + node kernels, 2 persistent task
         kernel, 3 fused (the automatic choice of step_kernel=0 resolved)."""
         return lib().ci_step_kernel(self._h)
+
+    def debug_flow_stall(self, chunk: int, wait_seconds: float) -> None:
+        """Test hook (ci_debug_flow_stall): the next task-kernel launch never publishes
+        chunk `chunk`'s progress, so its waits give up after wait_seconds."""
+        check(lib().ci_debug_flow_stall(self._h, int(chunk), float(wait_seconds)))
 
 
 class Batch:

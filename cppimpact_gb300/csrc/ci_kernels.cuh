@@ -1256,7 +1256,7 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
 // stale L1 line.  A task publishes its completion with a release store after a
 // __threadfence; the lanes of warp 0 read a task's neighbours' counters with acquire
 // loads, one neighbour per lane.  Every wait is bounded
-// in time (kFlowWaitNs): past it the CTA sets ST_FLOW_TIMEOUT and the abort flag, and
+// in time (wait_ns, 2 s by default): past it the CTA sets ST_FLOW_TIMEOUT and the abort flag, and
 // every CTA stops at its next claim or wait.
 struct FlowArgs {
   FusedArgs A[2];        // buffers of an even / odd step: state cur/prv, halo cur/prv
@@ -1275,9 +1275,11 @@ struct FlowArgs {
   int* abort_flag;
   int C;
   int nsteps;
+  unsigned long long wait_ns;  // a wait gives up after this long without progress
+  int stall_chunk;             // test hook: this chunk never publishes (-1: none)
 };
 
-constexpr unsigned long long kFlowWaitNs = 2000000000ull;  // 2 s without the awaited progress
+constexpr unsigned long long kFlowWaitNs = 2000000000ull;  // default: 2 s without progress
 constexpr int kFlowDescCount = 9;
 constexpr int kFlowDescChunk = 10;
 constexpr int kFlowDescHead = 12;
@@ -1318,7 +1320,7 @@ __device__ __forceinline__ bool flow_wait(const FlowArgs& F, const int* ctr, con
         }
         const unsigned long long t = global_ns();
         if (t0 == 0) t0 = t;
-        if (t - t0 > kFlowWaitNs) {
+        if (t - t0 > F.wait_ns) {
           atomicOr(F.A[0].status, (unsigned)ST_FLOW_TIMEOUT);
           atomicExch(F.abort_flag, 1);
           ok = false;
@@ -1570,11 +1572,11 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_flow_qp10(FlowArgs F, ElemPara
       node_epilogue<BS>(F.A[j & 1], ch, T, threadIdx.x);
       if (ep.accum_energy) add_chunk_work<BS>(F.A[0], c, wint, wp, red);
       __syncthreads();
-      if (threadIdx.x == BS - 32) flow_publish(F.elem_done, c, j);
+      if (threadIdx.x == BS - 32 && c != F.stall_chunk) flow_publish(F.elem_done, c, j);
     } else {
       flow_nodes<BS>(F, ep, np, ch, j);
       __syncthreads();
-      if (threadIdx.x == BS - 32) flow_publish(F.node_done, c, j);
+      if (threadIdx.x == BS - 32 && c != F.stall_chunk) flow_publish(F.node_done, c, j);
     }
   }
   if (w0) cp_async_wait();

@@ -126,6 +126,8 @@ struct ci_solver {
   DBuf<float4> d_rec;  // task kernel records: [2][N] float4 then [2][N] float2
   DBuf<int> d_flow_desc, d_flow_ctr;
   int flow_ctas = 0, flow_stride = 0;
+  unsigned long long flow_wait_ns = ci::kFlowWaitNs;
+  int flow_stall_chunk = -1;  // test hook, for the next task-kernel launch only
   size_t flow_smem = 0;
   bool xc_stale = true;  // X changed since d_Xc was uploaded
   // nodal strain/stress output: last element (caller order) of every node, and the plan
@@ -616,6 +618,10 @@ cudaError_t enqueue_flow(ci_solver* s, int n) {
     F.abort_flag = s->d_flow_ctr.p + 2 * C + 1;
     F.C = C;
     F.nsteps = k;
+    F.wait_ns = s->flow_wait_ns;
+    F.stall_chunk = s->flow_stall_chunk;
+    s->flow_stall_chunk = -1;
+    s->flow_wait_ns = ci::kFlowWaitNs;
     cudaError_t e;
     // progress counters to -1, task counter and abort flag to 0
     if ((e = cudaMemsetAsync(s->d_flow_ctr.p, 0xff, sizeof(int) * 2 * (size_t)C, s->stream))) return e;
@@ -1632,6 +1638,16 @@ int ci_time_kernels(ci_solver* s, int nsteps, float* out_ms) {
 }
 
 int ci_step_kernel(const ci_solver* s) { return s ? s->opt.step_kernel : -1; }
+
+int ci_debug_flow_stall(ci_solver* s, int chunk, double wait_seconds) {
+  if (!s) return fail(CI_ERR_INVALID, "null solver");
+  if (s->opt.step_kernel != 2) return fail(CI_ERR_UNSUPPORTED, "the solver does not run the task kernel");
+  if (chunk < 0 || chunk >= s->C || !(wait_seconds > 0.0) || wait_seconds > 60.0)
+    return fail(CI_ERR_INVALID, "bad chunk or wait");
+  s->flow_stall_chunk = chunk;
+  s->flow_wait_ns = (unsigned long long)(wait_seconds * 1e9);
+  return CI_OK;
+}
 
 int ci_launches_per_step(const ci_solver* s) {
   // the task kernel launches once per call of any length (and per 65,536 steps)

@@ -330,6 +330,14 @@ int ci_launches_per_step(const ci_solver* s);
 /* The step kernel a solver runs (ci_options::step_kernel with 0 resolved), -1 for NULL. */
 int ci_step_kernel(const ci_solver* s);
 
+/* Test hook for the task kernel's bounded waits: in the next launch (the next ci_step /
+ * ci_solve call) chunk `chunk` never publishes its progress, so the tasks waiting for it
+ * give up after wait_seconds (0 < wait_seconds <= 60), set the abort flag for the others
+ * and the call returns CI_ERR_CUDA ("a task waited longer than its time limit") with the
+ * CUDA context intact; the solver's state is then partial.  CI_ERR_UNSUPPORTED unless
+ * the solver runs the task kernel. */
+int ci_debug_flow_stall(ci_solver* s, int chunk, double wait_seconds);
+
 /* ---- mesh utilities (host only) ---- */
 /* Mesh::load_mesh (include/mesh.h:57-267): parse an Abaqus/CalculiX .inp file.
  * Arrays are malloc'ed by the library and released with ci_mesh_free. */

@@ -5,6 +5,8 @@ reference fixtures.  Tolerances (FP32 element math, FP64 nodal state):
     relative L2 of the FP64 run; identical contact-node sets (ever touched)."""
 import json
 
+import time
+
 import numpy as np
 import pytest
 
@@ -414,6 +416,40 @@ def test_task_kernel_long_launch_on_the_shell(cilib):
     assert ((a["contact"] & 2) > 0).sum() > 0, "the run must reach the plane"
     for k in ("x", "v", "contact"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_task_kernel_wait_times_out_and_reports(cilib):
+    """The task kernel's waits are bounded: with one chunk's progress never published
+    (the test hook), the tasks waiting for it give up after 0.2 s, every CTA returns, the
+    call reports CI_ERR_CUDA with the time-limit message, and the context stays usable --
+    a new solver on the same device then steps to the fused kernel's bits."""
+    m = mg.cube(6, 2)
+    setup = mg.impact_setup(m, 20.0, 1e-4)
+
+    def make(sk):
+        s = solver(cilib, m, cilib.MODE_J2, wall_normal=setup["wall_normal"],
+                   wall_offset=setup["wall_offset"], wall_stiffness=setup["wall_stiffness"],
+                   step_kernel=sk)
+        s.initialize(setup["vel"])
+        s.start(setup["dt"])
+        return s
+
+    s = make(2)
+    s.debug_flow_stall(3, 0.2)
+    t0 = time.perf_counter()
+    with pytest.raises(cilib.CiError) as e:
+        s.step(50)
+    assert e.value.code == -2 and "time limit" in str(e.value)
+    assert time.perf_counter() - t0 < 30.0
+    s.close()
+    out = []
+    for sk in (2, 3):
+        s = make(sk)
+        s.step(50)
+        out.append(s.state(("x", "v")))
+        s.close()
+    for k in ("x", "v"):
+        assert np.array_equal(out[0][k], out[1][k]), k
 
 
 def test_task_kernel_rejects_other_element_types(cilib):
