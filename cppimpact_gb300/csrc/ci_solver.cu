@@ -1046,8 +1046,12 @@ int ci_destroy(ci_solver* s) {
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   cudaStream_t st = s->stream;
+  const bool persisted = s->d_rec.p != nullptr;
   delete s;
   if (st) cudaStreamDestroy(st);
+  // lines the solver's access window kept in L2 return to normal use (the persisting
+  // limit itself belongs to this process's context and ends with it)
+  if (persisted) cudaCtxResetPersistingL2Cache();
   return CI_OK;
 }
 
