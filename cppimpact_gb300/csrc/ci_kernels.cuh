@@ -1509,7 +1509,8 @@ __device__ __forceinline__ void flow_stage(const FlowArgs& F, const ChunkInfo& c
 // which lands while t runs; after t, a thread of the last warp publishes while warp 0
 // already polls for the next task.  A task waits only for tasks earlier in the order,
 // and the earliest unfinished claimed task is always some CTA's current one, so holding
-// a claimed task cannot deadlock; all CTAs are resident (one round of the grid).  The
+// a claimed task cannot deadlock (only a running CTA claims, so this holds however many
+// CTAs are resident; the grid is one round of them).  The
 // loop keeps no counter: only shared memory carries state from one task to the next,
 // which leaves the element loop all 80 registers.
 template <int MODE, int BS>
