@@ -79,7 +79,7 @@ def workload(name: str):
 # kernel on the full shell (profiles/k_flow_qp10_shell.md: one launch of 20 steps,
 # divided by 20) and the fused kernel on the half shell (profiles/
 # k_step_qp10_shell_half.md, scaled x2 for the full shell: elements and nodes double).
-MEASURED_TRAFFIC = {("shell", 2): 6.938968e9 / 20, ("shell", 3): 2 * 117.996e6,
+MEASURED_TRAFFIC = {("shell", 2): 6.97644e9 / 20, ("shell", 3): 2 * 117.996e6,
                     ("shell_half", 3): 117.996e6}
 
 

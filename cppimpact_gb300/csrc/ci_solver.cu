@@ -42,6 +42,8 @@ int fail(int code, const char* fmt, ...) {
   } while (0)
 
 constexpr int kBS = 256;
+// local-node budget per chunk of the task kernel when the budget is automatic
+constexpr int kTaskChunkNodes = 768;
 
 template <typename T>
 struct DBuf {
@@ -966,20 +968,26 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   s->nq = s->npe == 4 ? 1 : 4;
   s->device = s->opt.device;
   CI_CUDA(cudaSetDevice(s->device));
-  std::string err;
-  if (!ci::build_plan(s->N, s->E, s->npe, mesh->xloc, mesh->element_nodes, s->opt.chunk_elements,
-                      s->opt.chunk_nodes, ci::kDefaultTargetCtas, &s->plan, &err))
-    return fail(CI_ERR_INVALID, "%s", err.c_str());
-  const ci::Plan& P = s->plan;
-  s->C = P.n_chunks;
-  s->S = P.slot_row[s->N];
-  s->Lt = (long long)P.local_gid.size();
-  // fused kernels: 40 B per local node (+ alignment); the element kernel: 36 B
-  s->smem_bytes = 40 * ((size_t)P.max_local + 2);
   int smem_max = 0;
   CI_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
-  if ((long long)s->smem_bytes + 1024 > smem_max)
-    return fail(CI_ERR_TOO_LARGE, "chunk needs %zu B of shared memory", s->smem_bytes);
+  // the plan and the sizes that follow from it (built again below with the task kernel's
+  // chunk budget when that kernel runs and the budget is automatic)
+  auto make_plan = [&](int chunk_nodes) -> int {
+    std::string err;
+    if (!ci::build_plan(s->N, s->E, s->npe, mesh->xloc, mesh->element_nodes,
+                        s->opt.chunk_elements, chunk_nodes, ci::kDefaultTargetCtas, &s->plan, &err))
+      return fail(CI_ERR_INVALID, "%s", err.c_str());
+    s->C = s->plan.n_chunks;
+    s->S = s->plan.slot_row[s->N];
+    s->Lt = (long long)s->plan.local_gid.size();
+    // fused kernels: 40 B per local node (+ alignment); the element kernel: 36 B
+    s->smem_bytes = 40 * ((size_t)s->plan.max_local + 2);
+    if ((long long)s->smem_bytes + 1024 > smem_max)
+      return fail(CI_ERR_TOO_LARGE, "chunk needs %zu B of shared memory", s->smem_bytes);
+    return CI_OK;
+  };
+  int rc;
+  if ((rc = make_plan(s->opt.chunk_nodes))) return rc;
   s->X0.assign(mesh->xloc, mesh->xloc + 3 * (size_t)s->N);
   s->X = s->X0;
   s->vel0.assign(3, 0.0);
@@ -999,10 +1007,17 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
       if (2LL * s->C > 3LL * per_sm * sms) s->opt.step_kernel = 2;
     }
   }
+  if (s->opt.step_kernel == 2 && s->opt.chunk_nodes == 0) {
+    // smaller chunks for the task kernel: six 768-node tiles per SM leave the SM a larger
+    // L1 for the read-only connectivity and index loads (shell: 98 against 107 us per
+    // step with the 896-node default, which suits the fused kernel)
+    if ((rc = make_plan(kTaskChunkNodes))) return rc;
+    CI_CUDA(configure_npe<10>((int)s->smem_bytes));
+  }
+  const ci::Plan& P = s->plan;
   CI_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   CI_CUDA(cudaEventCreate(&s->ev0));
   CI_CUDA(cudaEventCreate(&s->ev1));
-  int rc;
   if ((rc = upload(s->d_chunks, P.chunks, s->stream))) return rc;
   if ((rc = upload(s->d_conn, P.conn_local, s->stream))) return rc;
   if ((rc = upload(s->d_color, P.color, s->stream))) return rc;

@@ -395,17 +395,18 @@ def test_task_kernel_bitwise_equal_to_fused(cilib, mesh, mode, speed, calls):
 
 
 def test_task_kernel_long_launch_on_the_shell(cilib):
-    """The full shell (1,736 chunks, 912 resident CTAs) for 2,000 steps in one launch of
-    the task kernel -- 6.9 million tasks, each CTA moving through thousands of task
-    descriptors -- ends bit for bit where the fused kernel does.  A task that waited past
-    its time limit would raise here."""
+    """The full shell (2,067 chunks of at most 768 local nodes, 912 resident CTAs) for
+    2,000 steps in one launch of the task kernel -- 8.3 million tasks, each CTA moving
+    through thousands of task descriptors -- ends bit for bit where the fused kernel does
+    on the same plan (the task kernel's automatic 768-node chunk budget, given to both).
+    A task that waited past its time limit would raise here."""
     m = mg.shell()
     setup = mg.impact_setup(m, 5.0, 0.0)
     out = []
     for sk in (3, 2):
         s = solver(cilib, m, cilib.MODE_J2, wall_normal=setup["wall_normal"],
                    wall_offset=setup["wall_offset"], wall_stiffness=setup["wall_stiffness"],
-                   step_kernel=sk)
+                   step_kernel=sk, chunk_nodes=768)
         assert s.step_kernel() == sk
         s.initialize(setup["vel"])
         s.start(setup["dt"])
@@ -461,7 +462,8 @@ def test_task_kernel_rejects_other_element_types(cilib):
 
 def test_step_kernel_automatic_choice(cilib):
     """step_kernel = 0 picks the fused kernel for a mesh of about one round of CTAs and
-    the task kernel for a tet10 mesh of many (the full shell: 1,736 chunks)."""
+    the task kernel for a tet10 mesh of many (the full shell: 1,736 chunks of the default
+    896-node budget, planned again with the task kernel's 768)."""
     small = mg.cube(4, 2)
     s = solver(cilib, small, cilib.MODE_J2)
     assert s.step_kernel() == 3
