@@ -1233,7 +1233,9 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
 // Persistent task kernel of the four-lane tet10 step (step_kernel = 2).
 //
 // A call of n steps is one launch whose CTAs claim tasks from a counter, in the order
-//   N(0, c) for every chunk c;  then for j = 0 .. n-1:  E(j, c) for every c, N(j+1, c) for every c.
+//   N(0, .);  then for j = 0 .. n-1:  E(j, .), N(j+1, .),
+// each block in one task order of the chunks (reverse Cuthill-McKee on the graph of
+// chunks sharing a node, so that a task's dependencies lie about one block back).
 // N(j, c): chunk c completes S^j of the nodes it owns -- from S^{j-1} and the halo of step
 //   j-1 exactly as the fused kernel's staging does (N(0) reads the state as it is, N(n)
 //   also stores the accelerations) -- and writes each node's record (u and dt v rounded to
@@ -1245,19 +1247,19 @@ __global__ void __launch_bounds__(BS, 768 / BS) k_step_qp10(FusedArgs A, ElemPar
 // waits until every chunk with a slot of one of c's nodes has finished E(j-1, .).  These
 // waits order every reuse of the double buffers (records, halo, state) as well: E(j-2, t)
 // precedes N(j-1, c) precedes E(j-1, t) precedes N(j, c) for any chunk t touching c.  Every
-// dependency of a task comes earlier in the claim order and a claimed task runs on a
-// resident CTA, so the earliest unfinished task can always proceed.  Each node is
-// completed once (no ghost copies), and CTAs doing node tasks (memory and FP64 bound)
-// share the SMs with CTAs doing element tasks (FP32 issue bound).  The arithmetic is
-// the fused kernel's, so the results are the same bits.
+// dependency of a task comes earlier in the claim order and only a running CTA claims,
+// so the earliest unfinished task can always proceed.  Each node is completed once (no
+// ghost copies), and CTAs doing node tasks (memory and FP64 bound) share the SMs with
+// CTAs doing element tasks (FP32 issue bound).  The arithmetic is the fused kernel's, so
+// on the same plan the results are the same bits.
 //
-// Data written by other CTAs of the launch (records, halo, state, stored stress, work
-// sums, contact flags) is read through L2 only (ld.global.cg), never from a possibly
-// stale L1 line.  A task publishes its completion with a release store after a
-// __threadfence; the lanes of warp 0 read a task's neighbours' counters with acquire
-// loads, one neighbour per lane.  Every wait is bounded
-// in time (wait_ns, 2 s by default): past it the CTA sets ST_FLOW_TIMEOUT and the abort flag, and
-// every CTA stops at its next claim or wait.
+// Data written by other CTAs of the launch (records, halo, state, stored stress, contact
+// flags) is read through L2 only (ld.global.cg), never from a possibly stale L1 line; the
+// work sums are only added to (L2 reductions).  A task publishes its completion with a
+// release store after the CTA's last barrier; the lanes of warp 0 read a task's
+// neighbours' counters with acquire loads, one neighbour per lane.  Every wait is bounded
+// in time (wait_ns, 2 s by default): past it the CTA sets ST_FLOW_TIMEOUT and the abort
+// flag, and every CTA stops at its next wait.
 struct FlowArgs {
   FusedArgs A[2];        // buffers of an even / odd step: state cur/prv, halo cur/prv
   float4* rec_a[2];      // per node and parity: (u_x, u_y, u_z, dt v_x) in FP32
