@@ -995,16 +995,17 @@ int ci_create(const ci_mesh* mesh, const ci_material* mat, const ci_wall* wall,
   CI_CUDA(s->npe == 4 ? configure_npe<4>((int)s->smem_bytes) : configure_npe<10>((int)s->smem_bytes));
   if (s->opt.step_kernel == 0) {
     // automatic: the task kernel when the chunks of a four-lane tet10 mesh need more than
-    // 1.5 rounds of the fused kernel's resident CTAs (it then hides the lock-step of node
-    // staging and element loops; on meshes of about one round its waits cost more), else
-    // the fused kernel.  Both give the same bits.
+    // 0.8 of a round of the fused kernel's resident CTAs -- meshes whose chunks are cut by
+    // the local-node budget -- else the fused kernel (measured: the 604,800-element shell,
+    // 1.9 rounds, 98.0 against 121.9 us per step; half of it, 0.95 rounds, 58.1 against
+    // 63.4; the quad cube, 0.66 rounds of small chunks, 19.4 against 14.9).
     s->opt.step_kernel = 3;
     if (s->npe == 10 && s->opt.elem_lanes == 4 && s->opt.block_threads == 128) {
       int per_sm = 0, sms = 0;
       CI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
           &per_sm, ci::k_step_qp10<ci::EM_J2, 128>, 128, s->smem_bytes));
       CI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
-      if (2LL * s->C > 3LL * per_sm * sms) s->opt.step_kernel = 2;
+      if (5LL * s->C > 4LL * per_sm * sms) s->opt.step_kernel = 2;
     }
   }
   if (s->opt.step_kernel == 2 && s->opt.chunk_nodes == 0) {

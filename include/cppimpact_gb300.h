@@ -94,8 +94,8 @@ typedef struct ci_options {
   int chunk_elements; /* elements per CTA chunk, 0 = automatic */
   int chunk_nodes;    /* local-node budget per chunk, 0 = automatic */
   int graph_steps;    /* steps captured per CUDA graph, 0 = automatic */
-  int step_kernel;    /* 0 = automatic (2 for four-lane tet10 meshes of more than 1.5 rounds of
-                         fused CTAs, else 3), 1 = element + node kernels, 2 = persistent task
+  int step_kernel;    /* 0 = automatic (2 for four-lane tet10 meshes of more than 0.8 of a
+                         round of fused CTAs, else 3), 1 = element + node kernels, 2 = persistent task
                          kernel (tet10, elem_lanes 4, block_threads 128: node and element
                          tasks of all the call's steps), 3 = fused (one launch per step);
                          0, 2 and 3 give the same bits */

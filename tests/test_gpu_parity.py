@@ -461,14 +461,13 @@ def test_task_kernel_rejects_other_element_types(cilib):
 
 
 def test_step_kernel_automatic_choice(cilib):
-    """step_kernel = 0 picks the fused kernel for a mesh of about one round of CTAs and
-    the task kernel for a tet10 mesh of many (the full shell: 1,736 chunks of the default
-    896-node budget, planned again with the task kernel's 768)."""
-    small = mg.cube(4, 2)
-    s = solver(cilib, small, cilib.MODE_J2)
-    assert s.step_kernel() == 3
-    s.close()
-    shell = mg.shell()
-    s = solver(cilib, shell, cilib.MODE_J2)
-    assert s.step_kernel() == 2
-    s.close()
+    """step_kernel = 0 picks the fused kernel for a mesh of small chunks (the quad cube:
+    604 chunks, 0.66 of a round of CTAs) and the task kernel for tet10 meshes whose
+    chunks the local-node budget cuts (half the shell: 868 chunks, 0.95 of a round; the
+    full shell: 1,736 chunks of the default 896-node budget, planned again with the
+    task kernel's 768)."""
+    for m, sk in ((mg.cube(4, 2), 3), (mg.cube(18, 2), 3), (mg.shell(n_theta=360), 2),
+                  (mg.shell(), 2)):
+        s = solver(cilib, m, cilib.MODE_J2)
+        assert s.step_kernel() == sk
+        s.close()
