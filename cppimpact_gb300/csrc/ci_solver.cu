@@ -565,14 +565,17 @@ int setup_flow(ci_solver* s) {
   CI_CUDA(s->d_rec.alloc(3 * (size_t)s->N));
   {
     // the records go from a node task to the element tasks of the same step: keep them
-    // in L2 (a persisting access window over the one allocation)
+    // in L2 (a persisting access window over the one allocation).  Best effort: where the
+    // device or its partitioning offers no persisting L2, the solver runs without it.
     int max_persist = 0, max_window = 0;
-    CI_CUDA(cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, s->device));
-    CI_CUDA(cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, s->device));
     const size_t bytes = sizeof(float4) * 3 * (size_t)s->N;
-    if (max_persist > 0 && max_window > 0) {
+    bool ok = cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, s->device) ==
+                  cudaSuccess &&
+              cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, s->device) ==
+                  cudaSuccess &&
+              max_persist > 0 && max_window > 0;
+    if (ok) {
       const size_t limit = std::min(bytes, (size_t)max_persist);
-      CI_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, limit));
       cudaStreamAttrValue attr = {};
       attr.accessPolicyWindow.base_ptr = s->d_rec.p;
       attr.accessPolicyWindow.num_bytes = std::min(bytes, (size_t)max_window);
@@ -580,8 +583,11 @@ int setup_flow(ci_solver* s) {
           (float)std::min(1.0, (double)limit / (double)attr.accessPolicyWindow.num_bytes);
       attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
       attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-      CI_CUDA(cudaStreamSetAttribute(s->stream, cudaStreamAttributeAccessPolicyWindow, &attr));
+      ok = cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, limit) == cudaSuccess &&
+           cudaStreamSetAttribute(s->stream, cudaStreamAttributeAccessPolicyWindow, &attr) ==
+               cudaSuccess;
     }
+    if (!ok) cudaGetLastError();  // not an error of the solver's: clear it
   }
   CI_CUDA(s->d_flow_ctr.alloc(2 * (size_t)C + 2));
   auto kern = s->opt.mode != CI_MODE_REFCOMPAT ? ci::k_flow_qp10<ci::EM_J2, 128>
