@@ -426,6 +426,58 @@ bool verify_plan(const Plan& P, const int* conn, std::string* err) {
       *err = "slot not written exactly once";
       return false;
     }
+  // the task kernel's dependency lists: own(c) holds exactly the owners of c's local nodes
+  // (so an element task waits for every node task whose records it reads), touch(o)
+  // exactly the chunks whose own list holds o (so a node task waits for every element
+  // task that writes one of its nodes' halo slots), and the task order is a permutation
+  std::vector<int> own_row, own_idx, touch_row, touch_idx;
+  flow_lists(P, &own_row, &own_idx, &touch_row, &touch_idx);
+  const int C = P.n_chunks;
+  std::vector<int> owner(P.N, -1);
+  for (int c = 0; c < C; c++)
+    for (int l = 0; l < P.chunks[c].n_own; l++) owner[P.chunks[c].own_begin + l] = c;
+  std::vector<int> mark(C, -1);
+  for (int c = 0; c < C; c++) {
+    const ChunkInfo& ch = P.chunks[c];
+    int expect = 0;
+    for (int l = 0; l < ch.n_local; l++) {
+      const int o = owner[P.local_gid[ch.local_begin + l]];
+      if (o < 0 || o > c) {
+        *err = "a node's owner is not the first chunk touching it";
+        return false;
+      }
+      if (mark[o] != c) {
+        mark[o] = c;
+        expect++;
+      }
+    }
+    if (own_row[c + 1] - own_row[c] != expect) {
+      *err = "own list does not match the owners of the chunk's nodes";
+      return false;
+    }
+    for (int k = own_row[c]; k < own_row[c + 1]; k++) {
+      const int o = own_idx[k];
+      if (mark[o] != c) {
+        *err = "own list names a chunk owning none of the chunk's nodes";
+        return false;
+      }
+      if (!std::binary_search(touch_idx.begin() + touch_row[o], touch_idx.begin() + touch_row[o + 1], c)) {
+        *err = "touch list misses a chunk holding one of the owner's nodes";
+        return false;
+      }
+    }
+  }
+  if (own_idx.size() != touch_idx.size()) {
+    *err = "own and touch lists are not each other's transpose";
+    return false;
+  }
+  std::vector<int> order = flow_order(C, own_row, own_idx);
+  std::sort(order.begin(), order.end());
+  for (int k = 0; k < C; k++)
+    if (order[k] != k) {
+      *err = "task order of the chunks is not a permutation";
+      return false;
+    }
   return true;
 }
 

@@ -353,7 +353,9 @@ void ci_mesh_free(ci_mesh* m);
 int ci_plan_stats(const ci_mesh* mesh, int chunk_elements, int chunk_nodes, long long* stats,
                   int* perm_elems, int* perm_nodes);
 /* Check a plan's invariants on the host: every element once, colours conflict-free
- * within each chunk, slot lists cover every (chunk, node) pair.  Returns CI_OK. */
+ * within each chunk, slot lists cover every (chunk, node) pair, and the task kernel's
+ * dependency lists (each chunk's node owners and their transpose) and chunk task order
+ * are complete and consistent.  Returns CI_OK. */
 int ci_plan_verify(const ci_mesh* mesh, int chunk_elements, int chunk_nodes);
 
 #ifdef __cplusplus

@@ -62,6 +62,14 @@ def test_plan_is_deterministic_and_bijective(cilib):
     assert a["max_colors"] <= 64
 
 
+@pytest.mark.parametrize("chunk_nodes", [896, 768])
+def test_plan_invariants_on_the_shell(cilib, chunk_nodes):
+    """The full shell's plans under both automatic chunk budgets (the fused kernel's 896
+    local nodes, the task kernel's 768), including the task kernel's dependency lists."""
+    s = mg.shell()
+    cilib.plan_verify(s.xloc, s.conn, 0, chunk_nodes)
+
+
 def test_plan_shell_workload_shape(cilib):
     s = mg.shell()
     assert (s.num_elements, s.num_nodes) == (604800, 1213920)
