@@ -92,7 +92,8 @@ typedef struct ci_options {
   double gravity[3];  /* body acceleration; the reference uses (0, 0, -9.81) */
   int device;         /* CUDA device ordinal */
   int chunk_elements; /* elements per CTA chunk, 0 = automatic */
-  int chunk_nodes;    /* local-node budget per chunk, 0 = automatic */
+  int chunk_nodes;    /* local-node budget per chunk, 0 = automatic (896; 768 when the
+                         task kernel runs) */
   int graph_steps;    /* steps captured per CUDA graph, 0 = automatic */
   int step_kernel;    /* 0 = automatic (2 for four-lane tet10 meshes of more than 0.8 of a
                          round of fused CTAs, else 3), 1 = element + node kernels, 2 = persistent task
